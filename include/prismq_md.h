@@ -1,0 +1,243 @@
+/*
+ * prismq_md.h — C ABI of the GB300-native Prism-Q classical MD step.
+ *
+ * The library (libprismq_md.so) implements, as hand-written sm_103a CUDA
+ * kernels, the hot path of Prism-Q's NhsAmberFusedEngine:
+ *   cell-list neighbour build, AMBER ff14SB bonded forces, 10 Å potential-
+ *   shifted vacuum Coulomb + Lennard-Jones, the BAOAB/OVRVO Langevin phases
+ *   (OU, kick, drift) with SHAKE/RATTLE on X–H bonds under HMR.
+ *
+ * Conventions
+ *   - Units are the reference engine's: Å, ps, amu, kcal/mol, e.
+ *   - Positions, velocities and forces cross this boundary as host AoS
+ *     float[3*N] (x0,y0,z0,x1,...), the layout of NhsAmberFusedEngine's
+ *     get_positions/get_velocities (crates/prism-nhs/src/fused_engine.rs:24117,
+ *     :20939).  Internally the library keeps SoA float4 streams and int64
+ *     fixed-point forces at 2^-32 kcal/mol/Å.
+ *   - Every call returns a prismq_status; PRISMQ_OK is 0.  Device-side
+ *     failures (constraint non-convergence, list overflow, ...) never trap:
+ *     they set a per-system status word that the next host call reports.
+ *     prismq_last_error() returns the calling thread's last message.
+ *   - The library owns all device memory.  Caller buffers are host memory.
+ *   - A system or batch handle is externally synchronised (one thread at a
+ *     time); a server handle is internally locked.
+ *   - Pointers passed in a prismq_topology are read during the call only.
+ */
+#ifndef PRISMQ_MD_H
+#define PRISMQ_MD_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PRISMQ_ABI_VERSION 1
+
+typedef enum prismq_status {
+  PRISMQ_OK = 0,
+  PRISMQ_E_INVALID = 1,          /* bad argument / topology (host validation) */
+  PRISMQ_E_CUDA = 2,             /* CUDA runtime error */
+  PRISMQ_E_NO_DEVICE = 3,        /* no CUDA device visible */
+  PRISMQ_E_CAPACITY = 4,         /* caller buffer or arena too small */
+  PRISMQ_E_CELL_OVERFLOW = 5,    /* a cell held more atoms than the grid allows */
+  PRISMQ_E_NEIGHBOR_OVERFLOW = 6,/* an atom had more neighbours than the row holds */
+  PRISMQ_E_SHAKE = 7,            /* SHAKE did not converge in max_iter */
+  PRISMQ_E_RATTLE = 8,           /* RATTLE did not converge in max_iter */
+  PRISMQ_E_NONFINITE = 9,        /* NaN/Inf in state or forces */
+  PRISMQ_E_BUSY = 10,            /* server queue full */
+  PRISMQ_E_NOT_FOUND = 11
+} prismq_status;
+
+/* ---- topology (mirrors PrismPrepTopology, crates/prism-nhs/src/input.rs:1027-1140) ---- */
+
+typedef struct prismq_bond {      /* input.rs:230 BondParam; U = k (r - r0)^2 (k pre-halved) */
+  int32_t i, j;
+  float r0, k;
+} prismq_bond;
+
+typedef struct prismq_angle {     /* input.rs:243 AngleParam; U = k (θ - θ0)^2, θ in radians */
+  int32_t i, j, k;
+  float theta0, force_k;
+} prismq_angle;
+
+typedef struct prismq_dihedral {  /* input.rs:541 DihedralParam; U = k (1 + cos(nφ - γ)) */
+  int32_t i, j, k, l;
+  int32_t periodicity;
+  float phase, force_k;
+} prismq_dihedral;
+
+typedef struct prismq_exception { /* input.rs:581 NonbondedExceptionParam (exact 1-4 pair) */
+  int32_t i, j;
+  float charge_product;           /* e^2 */
+  float sigma;                    /* Å */
+  float epsilon;                  /* kcal/mol */
+} prismq_exception;
+
+typedef struct prismq_hcluster {  /* input.rs:625 HCluster */
+  int32_t central_atom;
+  int32_t hydrogen_atoms[3];      /* -1 for unused slots */
+  float bond_lengths[3];
+  int32_t n_hydrogens;            /* 1..3 */
+  float inv_mass_central;
+  float inv_mass_h;
+} prismq_hcluster;
+
+typedef struct prismq_topology {
+  int32_t n_atoms;
+  const float* positions;         /* [3N] Å */
+  const float* masses;            /* [N] amu, already repartitioned (HMR) */
+  const float* charges;           /* [N] e */
+  const float* lj_sigma;          /* [N] Å */
+  const float* lj_epsilon;        /* [N] kcal/mol */
+  int32_t n_bonds;       const prismq_bond* bonds;
+  int32_t n_angles;      const prismq_angle* angles;
+  int32_t n_dihedrals;   const prismq_dihedral* dihedrals;
+  int32_t n_exceptions;  const prismq_exception* exceptions;
+  /* Exclusions per atom (CSR over atoms): every partner whose ordinary
+   * nonbonded pair is removed (1-2, 1-3 and the 1-4 pairs that carry an
+   * exception).  input.rs:1094 `exclusions: Vec<Vec<usize>>`. */
+  const int32_t* exclusion_offsets;  /* [N+1] */
+  const int32_t* exclusions;         /* [exclusion_offsets[N]] */
+  int32_t n_clusters;    const prismq_hcluster* clusters;
+} prismq_topology;
+
+/* ---- run parameters (engine defaults: fused_engine.rs:13278-13366, set_dt :15342) ---- */
+
+typedef enum prismq_nlist_mode {
+  PRISMQ_NLIST_COMPLETE = 0,  /* every pair with r^2 <= r_list^2 (brute-force equal) */
+  PRISMQ_NLIST_REF27 = 1      /* reference scheme: fixed 10 Å grid from the initial box,
+                                 27-cell stencil, r^2 <= 144 (nhs_neighbor_warp.cuh:10-121) */
+} prismq_nlist_mode;
+
+typedef struct prismq_params {
+  float dt;                   /* ps; 0.004 under HMR */
+  float temperature;          /* K */
+  float gamma;                /* ps^-1 (0 => Hamiltonian kicks, no OU noise) */
+  float cutoff;               /* Å, 10 */
+  float skin;                 /* Å, list radius = cutoff + skin */
+  int32_t rebuild_interval;   /* steps; a half-skin displacement trigger also rebuilds */
+  int32_t com_interval;       /* steps between COM-velocity removals (100; 0 = never) */
+  int32_t max_constraint_iter;/* SHAKE/RATTLE iteration bound (100) */
+  uint32_t seed;              /* Philox key word 0 */
+  uint32_t stream;            /* Philox key word 1 (system id in a batch) */
+} prismq_params;
+
+/* Fill *p with the reference engine defaults under HMR
+ * (dt 0.004, T 300, γ 1, cutoff 10, skin 2, rebuild 20, COM 100, 100 iterations). */
+void prismq_params_default(prismq_params* p);
+
+const char* prismq_last_error(void);
+int prismq_abi_version(void);
+/* Number of CUDA devices visible (0 without a GPU); never fails. */
+int prismq_device_count(void);
+/* Kernels this library has launched in this process (graph nodes counted). */
+long long prismq_kernel_launches(void);
+
+/* ---- synthetic poly-alanine-like systems (host only, no GPU) ---- */
+
+typedef struct prismq_topology_buf prismq_topology_buf;
+
+/* Build n_chains seeded chains of n_residues each (10 atoms/residue: N H CA HA
+ * CB HB1 HB2 HB3 C O; ff14SB ALA charges/LJ/bonded terms; exact 1-4
+ * exceptions qq/1.2, σ̄, ε̄/2; HMR with hydrogen mass 3.024 amu).
+ * Each chain grows inside its own region: a sphere of atom density `density`
+ * (atoms/Å^3; <= 0 selects 0.03) when box_edge <= 0, otherwise one cell of a
+ * box of edge box_edge split among the chains.  Self-avoiding growth with
+ * ideal internal coordinates stalls above ~0.035 atoms/Å^3, so a region that
+ * is too dense is enlarged by 5% per attempt.  Deterministic for a given
+ * seed, with identical bits on x86-64 and aarch64. */
+prismq_status prismq_polyala_build(int32_t n_chains, int32_t n_residues, uint64_t seed,
+                                   float density, float box_edge,
+                                   prismq_topology_buf** out);
+/* View the arrays of a built topology; valid until prismq_topology_free. */
+prismq_status prismq_topology_view(const prismq_topology_buf* buf, prismq_topology* out);
+void prismq_topology_free(prismq_topology_buf* buf);
+
+/* ---- single system (the drop-in for NhsAmberFusedEngine, fused_engine.rs:6554) ---- */
+
+typedef struct prismq_system prismq_system;
+
+/* NhsAmberFusedEngine::new_on_stream (fused_engine.rs:10800): validate and
+ * lower the topology (exception CSR :11625-11700, incidence :11704-11745,
+ * H clusters :11827-11938, cell grid :12285-12330), upload, and initialise
+ * Maxwell–Boltzmann velocities at params->temperature with COM removed. */
+prismq_status prismq_system_create(const prismq_topology* topo, const prismq_params* params,
+                                   prismq_system** out);
+void prismq_system_destroy(prismq_system* sys);
+int32_t prismq_system_n_atoms(const prismq_system* sys);
+
+/* set_dt (fused_engine.rs:15342) and friends; take effect at the next step. */
+prismq_status prismq_set_dt(prismq_system* sys, float dt);
+prismq_status prismq_set_temperature(prismq_system* sys, float temperature);
+prismq_status prismq_set_gamma(prismq_system* sys, float gamma);
+
+/* Host AoS float[3N] in/out (get_positions :24117, get_velocities :20939). */
+prismq_status prismq_set_positions(prismq_system* sys, const float* xyz);
+prismq_status prismq_set_velocities(prismq_system* sys, const float* vxyz);
+prismq_status prismq_get_positions(prismq_system* sys, float* xyz);
+prismq_status prismq_get_velocities(prismq_system* sys, float* vxyz);
+/* Step counter (the value of `timestep` before the next step). */
+prismq_status prismq_get_step(prismq_system* sys, int64_t* step);
+prismq_status prismq_set_step(prismq_system* sys, int64_t step);
+
+/* Force evaluation at the current positions (FORCE_N phase, nhs_amber_fused.cu:2993-3484).
+ * pe_total: FP64 total potential energy (may be NULL).
+ * f_aos: float[3N] kcal/mol/Å (may be NULL).  f_fixed: int64[3N] at 2^-32 (may be NULL). */
+prismq_status prismq_compute_forces(prismq_system* sys, double* pe_total, float* f_aos,
+                                    int64_t* f_fixed);
+/* Energy components: [bond, angle, dihedral, exception, nonbonded(shifted), kinetic]. */
+prismq_status prismq_energy_components(prismq_system* sys, double out[6]);
+
+/* Build the pair list at the current positions and return the canonical
+ * (i<j) pairs, sorted, as int32 pairs_out[2*n].  REF27 reproduces the
+ * reference pair set (exclusion CSR = exclusions minus exception pairs);
+ * COMPLETE returns every pair with r^2 <= (cutoff+skin)^2 in the same FP32
+ * arithmetic.  *n receives the number of pairs; PRISMQ_E_CAPACITY if
+ * cap < n (n still reported). */
+prismq_status prismq_build_neighbors(prismq_system* sys, prismq_nlist_mode mode,
+                                     int32_t* pairs_out, size_t cap, size_t* n);
+
+/* Advance n_steps MD steps (step(), fused_engine.rs:18963, phase order
+ * MD_EXECUTION_PHASES :6223-6235 plus the post-step clamp/RATTLE :17498-17800). */
+prismq_status prismq_step(prismq_system* sys, int64_t n_steps);
+
+/* Debug entry points used by the parity tests (single phases on the device). */
+typedef enum prismq_phase_set {
+  PRISMQ_PHASES_PRE = 1,   /* OU½ → RATTLE → KICK½ → RATTLE → DRIFT → SHAKE */
+  PRISMQ_PHASES_POST = 2   /* KICK½ → RATTLE → OU½ → velocity clamp → RATTLE */
+} prismq_phase_set;
+/* Run one phase set with the current forces, using noise for step `step`. */
+prismq_status prismq_debug_phases(prismq_system* sys, prismq_phase_set set, int64_t step);
+/* Host copy of the injected noise: three normals per atom for (seed, stream,
+ * atom, step, purpose) — bit-identical to what the kernels draw. */
+void prismq_debug_noise(uint32_t seed, uint32_t stream, uint32_t atom, uint64_t step,
+                        uint32_t purpose, float out3[3]);
+
+/* ---- batch: many independent systems advanced together ---- */
+
+typedef struct prismq_batch prismq_batch;
+
+/* Create an empty batch with room for max_atoms atoms in total. */
+prismq_status prismq_batch_create(int64_t max_atoms, int32_t max_systems, prismq_batch** out);
+void prismq_batch_destroy(prismq_batch* b);
+/* Admit a system; *slot receives its index.  PRISMQ_E_CAPACITY if it does not fit. */
+prismq_status prismq_batch_add_system(prismq_batch* b, const prismq_topology* topo,
+                                      const prismq_params* params, int32_t* slot);
+prismq_status prismq_batch_remove_system(prismq_batch* b, int32_t slot);
+/* Advance every resident system by n_steps (one captured CUDA graph per step). */
+prismq_status prismq_batch_step(prismq_batch* b, int64_t n_steps);
+prismq_status prismq_batch_get_state(prismq_batch* b, int32_t slot, float* xyz, float* vxyz);
+prismq_status prismq_batch_set_state(prismq_batch* b, int32_t slot, const float* xyz,
+                                     const float* vxyz);
+prismq_status prismq_batch_get_step(prismq_batch* b, int32_t slot, int64_t* step);
+prismq_status prismq_batch_status(prismq_batch* b, int32_t slot);
+prismq_status prismq_batch_energy(prismq_batch* b, int32_t slot, double out[6]);
+int64_t prismq_batch_resident_atoms(const prismq_batch* b);
+int32_t prismq_batch_resident_systems(const prismq_batch* b);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PRISMQ_MD_H */

@@ -1,0 +1,456 @@
+"""GB300-native Prism-Q classical MD step — Python host API over the C ABI.
+
+The compute path is libprismq_md.so (hand-written sm_103a CUDA, built in-tree
+by build.py); this module is a thin ctypes layer that mirrors the reference
+engine's interface (NhsAmberFusedEngine, crates/prism-nhs/src/fused_engine.rs:
+new_on_stream :10800, set_dt :15342, step :18963, run :23911,
+rebuild_neighbor_lists :16615, get_positions :24117, get_velocities :20939)
+with the same argument meaning.  Errors raise PrismQError carrying the C
+status code; there is no CPU fallback — without the built library or a GPU,
+calls fail loudly.
+"""
+from __future__ import annotations
+
+import ctypes
+import pathlib
+from dataclasses import dataclass
+
+import numpy as np
+
+_HERE = pathlib.Path(__file__).resolve().parent
+LIB_PATH = _HERE / "libprismq_md.so"
+HEADER = _HERE.parent / "include" / "prismq_md.h"
+
+STATUS = {
+    0: "OK", 1: "E_INVALID", 2: "E_CUDA", 3: "E_NO_DEVICE", 4: "E_CAPACITY", 5: "E_CELL_OVERFLOW",
+    6: "E_NEIGHBOR_OVERFLOW", 7: "E_SHAKE", 8: "E_RATTLE", 9: "E_NONFINITE", 10: "E_BUSY",
+    11: "E_NOT_FOUND",
+}
+NLIST_COMPLETE, NLIST_REF27 = 0, 1
+PHASES_PRE, PHASES_POST = 1, 2
+
+
+class PrismQError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+# ---------------------------------------------------------------- C structs
+class Bond(ctypes.Structure):
+    _fields_ = [("i", ctypes.c_int32), ("j", ctypes.c_int32), ("r0", ctypes.c_float), ("k", ctypes.c_float)]
+
+
+class Angle(ctypes.Structure):
+    _fields_ = [("i", ctypes.c_int32), ("j", ctypes.c_int32), ("k", ctypes.c_int32),
+                ("theta0", ctypes.c_float), ("force_k", ctypes.c_float)]
+
+
+class Dihedral(ctypes.Structure):
+    _fields_ = [("i", ctypes.c_int32), ("j", ctypes.c_int32), ("k", ctypes.c_int32), ("l", ctypes.c_int32),
+                ("periodicity", ctypes.c_int32), ("phase", ctypes.c_float), ("force_k", ctypes.c_float)]
+
+
+class Exception14(ctypes.Structure):
+    _fields_ = [("i", ctypes.c_int32), ("j", ctypes.c_int32), ("charge_product", ctypes.c_float),
+                ("sigma", ctypes.c_float), ("epsilon", ctypes.c_float)]
+
+
+class HCluster(ctypes.Structure):
+    _fields_ = [("central_atom", ctypes.c_int32), ("hydrogen_atoms", ctypes.c_int32 * 3),
+                ("bond_lengths", ctypes.c_float * 3), ("n_hydrogens", ctypes.c_int32),
+                ("inv_mass_central", ctypes.c_float), ("inv_mass_h", ctypes.c_float)]
+
+
+_P = ctypes.c_void_p
+
+
+class TopologyStruct(ctypes.Structure):
+    _fields_ = [("n_atoms", ctypes.c_int32), ("positions", _P), ("masses", _P), ("charges", _P),
+                ("lj_sigma", _P), ("lj_epsilon", _P),
+                ("n_bonds", ctypes.c_int32), ("bonds", _P), ("n_angles", ctypes.c_int32), ("angles", _P),
+                ("n_dihedrals", ctypes.c_int32), ("dihedrals", _P),
+                ("n_exceptions", ctypes.c_int32), ("exceptions", _P),
+                ("exclusion_offsets", _P), ("exclusions", _P),
+                ("n_clusters", ctypes.c_int32), ("clusters", _P)]
+
+
+class ParamsStruct(ctypes.Structure):
+    _fields_ = [("dt", ctypes.c_float), ("temperature", ctypes.c_float), ("gamma", ctypes.c_float),
+                ("cutoff", ctypes.c_float), ("skin", ctypes.c_float), ("rebuild_interval", ctypes.c_int32),
+                ("com_interval", ctypes.c_int32), ("max_constraint_iter", ctypes.c_int32),
+                ("seed", ctypes.c_uint32), ("stream", ctypes.c_uint32)]
+
+
+# numpy dtypes with the same layout as the C structs
+BOND_DT = np.dtype([("i", "<i4"), ("j", "<i4"), ("r0", "<f4"), ("k", "<f4")])
+ANGLE_DT = np.dtype([("i", "<i4"), ("j", "<i4"), ("k", "<i4"), ("theta0", "<f4"), ("force_k", "<f4")])
+DIH_DT = np.dtype([("i", "<i4"), ("j", "<i4"), ("k", "<i4"), ("l", "<i4"), ("periodicity", "<i4"),
+                   ("phase", "<f4"), ("force_k", "<f4")])
+EXC_DT = np.dtype([("i", "<i4"), ("j", "<i4"), ("charge_product", "<f4"), ("sigma", "<f4"), ("epsilon", "<f4")])
+CLUSTER_DT = np.dtype([("central_atom", "<i4"), ("hydrogen_atoms", "<i4", (3,)), ("bond_lengths", "<f4", (3,)),
+                       ("n_hydrogens", "<i4"), ("inv_mass_central", "<f4"), ("inv_mass_h", "<f4")])
+
+_lib = None
+
+
+def load() -> ctypes.CDLL:
+    """Load libprismq_md.so (built by build.py); raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise PrismQError(2, f"{LIB_PATH} is not built; run prism-q_gb300/build.py")
+    L = ctypes.CDLL(str(LIB_PATH))
+    I, P, i64 = ctypes.c_int, ctypes.c_void_p, ctypes.c_int64
+    sigs = {
+        "prismq_last_error": (ctypes.c_char_p, []),
+        "prismq_abi_version": (I, []),
+        "prismq_device_count": (I, []),
+        "prismq_kernel_launches": (ctypes.c_longlong, []),
+        "prismq_params_default": (None, [P]),
+        "prismq_polyala_build": (I, [ctypes.c_int32, ctypes.c_int32, ctypes.c_uint64, ctypes.c_float,
+                                     ctypes.c_float, P]),
+        "prismq_topology_view": (I, [P, P]),
+        "prismq_topology_free": (None, [P]),
+        "prismq_system_create": (I, [P, P, P]),
+        "prismq_system_destroy": (None, [P]),
+        "prismq_system_n_atoms": (ctypes.c_int32, [P]),
+        "prismq_set_dt": (I, [P, ctypes.c_float]),
+        "prismq_set_temperature": (I, [P, ctypes.c_float]),
+        "prismq_set_gamma": (I, [P, ctypes.c_float]),
+        "prismq_set_positions": (I, [P, P]),
+        "prismq_set_velocities": (I, [P, P]),
+        "prismq_get_positions": (I, [P, P]),
+        "prismq_get_velocities": (I, [P, P]),
+        "prismq_get_step": (I, [P, P]),
+        "prismq_set_step": (I, [P, i64]),
+        "prismq_compute_forces": (I, [P, P, P, P]),
+        "prismq_energy_components": (I, [P, P]),
+        "prismq_build_neighbors": (I, [P, I, P, ctypes.c_size_t, P]),
+        "prismq_step": (I, [P, i64]),
+        "prismq_debug_phases": (I, [P, I, i64]),
+        "prismq_debug_noise": (None, [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64,
+                                      ctypes.c_uint32, P]),
+        "prismq_batch_create": (I, [i64, ctypes.c_int32, P]),
+        "prismq_batch_destroy": (None, [P]),
+        "prismq_batch_add_system": (I, [P, P, P, P]),
+        "prismq_batch_remove_system": (I, [P, ctypes.c_int32]),
+        "prismq_batch_step": (I, [P, i64]),
+        "prismq_batch_get_state": (I, [P, ctypes.c_int32, P, P]),
+        "prismq_batch_set_state": (I, [P, ctypes.c_int32, P, P]),
+        "prismq_batch_get_step": (I, [P, ctypes.c_int32, P]),
+        "prismq_batch_status": (I, [P, ctypes.c_int32]),
+        "prismq_batch_energy": (I, [P, ctypes.c_int32, P]),
+        "prismq_batch_resident_atoms": (i64, [P]),
+        "prismq_batch_resident_systems": (ctypes.c_int32, [P]),
+    }
+    for name, (res, args) in sigs.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(rc: int) -> None:
+    if rc != 0:
+        msg = load().prismq_last_error()
+        raise PrismQError(rc, msg.decode() if msg else "")
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def device_count() -> int:
+    return load().prismq_device_count()
+
+
+def kernel_launches() -> int:
+    return int(load().prismq_kernel_launches())
+
+
+def debug_noise(seed: int, stream: int, atom: int, step: int, purpose: int) -> np.ndarray:
+    out = np.zeros(3, dtype=np.float32)
+    load().prismq_debug_noise(seed, stream, atom, step, purpose, _ptr(out))
+    return out
+
+
+# ---------------------------------------------------------------- parameters
+@dataclass
+class Params:
+    dt: float = 0.004
+    temperature: float = 300.0
+    gamma: float = 1.0
+    cutoff: float = 10.0
+    skin: float = 2.0
+    rebuild_interval: int = 20
+    com_interval: int = 100
+    max_constraint_iter: int = 100
+    seed: int = 0x50524953
+    stream: int = 0
+
+    def struct(self) -> ParamsStruct:
+        return ParamsStruct(self.dt, self.temperature, self.gamma, self.cutoff, self.skin,
+                            self.rebuild_interval, self.com_interval, self.max_constraint_iter,
+                            self.seed & 0xffffffff, self.stream & 0xffffffff)
+
+
+# ---------------------------------------------------------------- topology
+class Topology:
+    """Owned numpy copy of a prismq_topology (PrismPrepTopology field set)."""
+
+    def __init__(self, positions, masses, charges, lj_sigma, lj_epsilon, bonds=None, angles=None,
+                 dihedrals=None, exceptions=None, exclusion_offsets=None, exclusions=None, clusters=None):
+        self.positions = np.ascontiguousarray(positions, dtype=np.float32).reshape(-1, 3)
+        n = len(self.positions)
+        self.masses = np.ascontiguousarray(masses, dtype=np.float32).reshape(n)
+        self.charges = np.ascontiguousarray(charges, dtype=np.float32).reshape(n)
+        self.lj_sigma = np.ascontiguousarray(lj_sigma, dtype=np.float32).reshape(n)
+        self.lj_epsilon = np.ascontiguousarray(lj_epsilon, dtype=np.float32).reshape(n)
+        self.bonds = np.ascontiguousarray(bonds if bonds is not None else np.zeros(0, BOND_DT), dtype=BOND_DT)
+        self.angles = np.ascontiguousarray(angles if angles is not None else np.zeros(0, ANGLE_DT), dtype=ANGLE_DT)
+        self.dihedrals = np.ascontiguousarray(dihedrals if dihedrals is not None else np.zeros(0, DIH_DT),
+                                              dtype=DIH_DT)
+        self.exceptions = np.ascontiguousarray(exceptions if exceptions is not None else np.zeros(0, EXC_DT),
+                                               dtype=EXC_DT)
+        if exclusion_offsets is None:
+            exclusion_offsets = np.zeros(n + 1, np.int32)
+            exclusions = np.zeros(0, np.int32)
+        self.exclusion_offsets = np.ascontiguousarray(exclusion_offsets, dtype=np.int32)
+        self.exclusions = np.ascontiguousarray(exclusions, dtype=np.int32)
+        self.clusters = np.ascontiguousarray(clusters if clusters is not None else np.zeros(0, CLUSTER_DT),
+                                             dtype=CLUSTER_DT)
+
+    @property
+    def n_atoms(self) -> int:
+        return len(self.positions)
+
+    def struct(self) -> TopologyStruct:
+        t = TopologyStruct()
+        t.n_atoms = self.n_atoms
+        t.positions, t.masses, t.charges = _ptr(self.positions), _ptr(self.masses), _ptr(self.charges)
+        t.lj_sigma, t.lj_epsilon = _ptr(self.lj_sigma), _ptr(self.lj_epsilon)
+        t.n_bonds, t.bonds = len(self.bonds), _ptr(self.bonds)
+        t.n_angles, t.angles = len(self.angles), _ptr(self.angles)
+        t.n_dihedrals, t.dihedrals = len(self.dihedrals), _ptr(self.dihedrals)
+        t.n_exceptions, t.exceptions = len(self.exceptions), _ptr(self.exceptions)
+        t.exclusion_offsets, t.exclusions = _ptr(self.exclusion_offsets), _ptr(self.exclusions)
+        t.n_clusters, t.clusters = len(self.clusters), _ptr(self.clusters)
+        return t
+
+    @classmethod
+    def polyala(cls, n_chains: int = 1, n_residues: int = 250, seed: int = 1, density: float = 0.03,
+                box_edge: float = 0.0) -> "Topology":
+        """Seeded synthetic poly-alanine-like system (C generator in the library)."""
+        L = load()
+        buf = ctypes.c_void_p()
+        _check(L.prismq_polyala_build(n_chains, n_residues, seed, density, box_edge, ctypes.byref(buf)))
+        try:
+            t = TopologyStruct()
+            _check(L.prismq_topology_view(buf, ctypes.byref(t)))
+            n = t.n_atoms
+
+            def arr(ptr, count, dtype, shape=None):
+                if count == 0:
+                    return np.zeros(shape or 0, dtype=dtype)
+                nbytes = count * np.dtype(dtype).itemsize
+                raw = ctypes.string_at(ptr, nbytes)
+                a = np.frombuffer(raw, dtype=dtype).copy()
+                return a.reshape(shape) if shape else a
+
+            eoff = arr(t.exclusion_offsets, n + 1, np.int32)
+            return cls(arr(t.positions, 3 * n, np.float32, (n, 3)), arr(t.masses, n, np.float32),
+                       arr(t.charges, n, np.float32), arr(t.lj_sigma, n, np.float32),
+                       arr(t.lj_epsilon, n, np.float32), arr(t.bonds, t.n_bonds, BOND_DT),
+                       arr(t.angles, t.n_angles, ANGLE_DT), arr(t.dihedrals, t.n_dihedrals, DIH_DT),
+                       arr(t.exceptions, t.n_exceptions, EXC_DT), eoff,
+                       arr(t.exclusions, int(eoff[-1]), np.int32), arr(t.clusters, t.n_clusters, CLUSTER_DT))
+        finally:
+            L.prismq_topology_free(buf)
+
+    @classmethod
+    def point_cloud(cls, positions) -> "Topology":
+        """Atoms only (no bonded terms, exclusions or constraints): for neighbour-list parity."""
+        p = np.asarray(positions, dtype=np.float32).reshape(-1, 3)
+        n = len(p)
+        return cls(p, np.full(n, 12.0, np.float32), np.zeros(n, np.float32), np.full(n, 3.0, np.float32),
+                   np.full(n, 0.1, np.float32))
+
+
+# ---------------------------------------------------------------- engine
+class NhsAmberFusedEngine:
+    """One system on the GPU (the drop-in for the reference engine's MD step)."""
+
+    def __init__(self, topology: Topology, params: Params | None = None):
+        self.topology = topology
+        self.params = params or Params()
+        self._t = topology.struct()
+        self._p = self.params.struct()
+        self.h = ctypes.c_void_p()
+        _check(load().prismq_system_create(ctypes.byref(self._t), ctypes.byref(self._p), ctypes.byref(self.h)))
+        self.n_atoms = topology.n_atoms
+
+    # reference name: new_on_stream
+    @classmethod
+    def new_on_stream(cls, topology: Topology, params: Params | None = None) -> "NhsAmberFusedEngine":
+        return cls(topology, params)
+
+    def close(self) -> None:
+        if self.h:
+            load().prismq_system_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_dt(self, dt: float) -> None:
+        _check(load().prismq_set_dt(self.h, dt))
+
+    def set_temperature(self, t: float) -> None:
+        _check(load().prismq_set_temperature(self.h, t))
+
+    def set_gamma(self, g: float) -> None:
+        _check(load().prismq_set_gamma(self.h, g))
+
+    def step(self, n_steps: int = 1) -> None:
+        _check(load().prismq_step(self.h, n_steps))
+
+    def run(self, n_steps: int) -> None:
+        self.step(n_steps)
+
+    @property
+    def timestep(self) -> int:
+        v = ctypes.c_int64()
+        _check(load().prismq_get_step(self.h, ctypes.byref(v)))
+        return v.value
+
+    def set_timestep(self, step: int) -> None:
+        _check(load().prismq_set_step(self.h, step))
+
+    def get_positions(self) -> np.ndarray:
+        out = np.zeros((self.n_atoms, 3), np.float32)
+        _check(load().prismq_get_positions(self.h, _ptr(out)))
+        return out
+
+    def get_velocities(self) -> np.ndarray:
+        out = np.zeros((self.n_atoms, 3), np.float32)
+        _check(load().prismq_get_velocities(self.h, _ptr(out)))
+        return out
+
+    def set_positions(self, xyz) -> None:
+        a = np.ascontiguousarray(xyz, dtype=np.float32).reshape(-1)
+        _check(load().prismq_set_positions(self.h, _ptr(a)))
+
+    def set_velocities(self, vxyz) -> None:
+        a = np.ascontiguousarray(vxyz, dtype=np.float32).reshape(-1)
+        _check(load().prismq_set_velocities(self.h, _ptr(a)))
+
+    def compute_forces(self):
+        """(pe_total, forces float[N,3], forces_fixed int64[N,3]) at the current positions."""
+        pe = ctypes.c_double()
+        f = np.zeros((self.n_atoms, 3), np.float32)
+        fx = np.zeros((self.n_atoms, 3), np.int64)
+        _check(load().prismq_compute_forces(self.h, ctypes.byref(pe), _ptr(f), _ptr(fx)))
+        return pe.value, f, fx
+
+    def energy_components(self) -> np.ndarray:
+        """[bond, angle, dihedral, exception, nonbonded, kinetic] in kcal/mol (FP64)."""
+        out = np.zeros(6, np.float64)
+        _check(load().prismq_energy_components(self.h, _ptr(out)))
+        return out
+
+    def build_neighbors(self, mode: int = NLIST_COMPLETE) -> np.ndarray:
+        n = ctypes.c_size_t()
+        L = load()
+        rc = L.prismq_build_neighbors(self.h, mode, None, 0, ctypes.byref(n))
+        if rc not in (0, 4):
+            _check(rc)
+        out = np.zeros((max(n.value, 1), 2), np.int32)
+        _check(L.prismq_build_neighbors(self.h, mode, _ptr(out), n.value, ctypes.byref(n)))
+        return out[: n.value]
+
+    def rebuild_neighbor_lists(self) -> np.ndarray:
+        return self.build_neighbors(NLIST_REF27)
+
+    def debug_phases(self, which: int, step: int) -> None:
+        _check(load().prismq_debug_phases(self.h, which, step))
+
+
+class Batch:
+    """Many independent systems advanced together in one launch per phase."""
+
+    def __init__(self, max_atoms: int, max_systems: int):
+        self.h = ctypes.c_void_p()
+        _check(load().prismq_batch_create(max_atoms, max_systems, ctypes.byref(self.h)))
+        self.n_atoms: dict[int, int] = {}
+        self._keep: dict[int, tuple] = {}
+
+    def close(self) -> None:
+        if self.h:
+            load().prismq_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_system(self, topology: Topology, params: Params | None = None) -> int:
+        t = topology.struct()
+        p = (params or Params()).struct()
+        slot = ctypes.c_int32()
+        _check(load().prismq_batch_add_system(self.h, ctypes.byref(t), ctypes.byref(p), ctypes.byref(slot)))
+        self.n_atoms[slot.value] = topology.n_atoms
+        return slot.value
+
+    def remove_system(self, slot: int) -> None:
+        _check(load().prismq_batch_remove_system(self.h, slot))
+        self.n_atoms.pop(slot, None)
+
+    def step(self, n_steps: int = 1) -> None:
+        _check(load().prismq_batch_step(self.h, n_steps))
+
+    def get_state(self, slot: int):
+        n = self.n_atoms[slot]
+        x = np.zeros((n, 3), np.float32)
+        v = np.zeros((n, 3), np.float32)
+        _check(load().prismq_batch_get_state(self.h, slot, _ptr(x), _ptr(v)))
+        return x, v
+
+    def set_state(self, slot: int, x=None, v=None) -> None:
+        xa = None if x is None else np.ascontiguousarray(x, np.float32).reshape(-1)
+        va = None if v is None else np.ascontiguousarray(v, np.float32).reshape(-1)
+        _check(load().prismq_batch_set_state(self.h, slot, _ptr(xa), _ptr(va)))
+
+    def timestep(self, slot: int) -> int:
+        v = ctypes.c_int64()
+        _check(load().prismq_batch_get_step(self.h, slot, ctypes.byref(v)))
+        return v.value
+
+    def status(self, slot: int) -> int:
+        return load().prismq_batch_status(self.h, slot)
+
+    def energy(self, slot: int) -> np.ndarray:
+        out = np.zeros(6, np.float64)
+        _check(load().prismq_batch_energy(self.h, slot, _ptr(out)))
+        return out
+
+    @property
+    def resident_atoms(self) -> int:
+        return int(load().prismq_batch_resident_atoms(self.h))
+
+    @property
+    def resident_systems(self) -> int:
+        return int(load().prismq_batch_resident_systems(self.h))

@@ -1,0 +1,1201 @@
+// C ABI of the GB300 MD step: topology lowering, the batched device arena,
+// the per-step launch sequence and its CUDA graph.
+//
+// Host-side lowering restates the reference engine's constructor
+// (NhsAmberFusedEngine::new_on_stream_with_nonbonded_policy,
+// crates/prism-nhs/src/fused_engine.rs:10870):
+//   exception CSR, both directions, ascending partner       :11625-11680
+//   exclusion set = topology exclusions minus exception pairs :11680-11700
+//   incidence lists sorted by (term, position)              :11704-11745, :16034-16063
+//   H-cluster validation (cardinality, inverse masses, overlap) :11827-11938
+//   fixed reference grid from the initial bounding box       :12285-12330
+//   Maxwell–Boltzmann start velocities with COM removed      :16065-16100
+//
+// One step on the device is four launches, captured once per batch shape in a
+// CUDA graph:  control+cells (per system) → neighbour rows → forces →
+// integrate (post-phases of this step fused with pre-phases of the next).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "pq_common.cuh"
+#include "pq_device.cuh"
+#include "pq_host.h"
+
+using namespace pq;
+
+static thread_local std::string g_err;
+static std::atomic<long long> g_launches{0};
+
+static prismq_status fail(prismq_status st, const std::string& msg) {
+  g_err = msg;
+  return st;
+}
+
+#define PQ_CK(x)                                                                             \
+  do {                                                                                       \
+    cudaError_t e_ = (x);                                                                    \
+    if (e_ != cudaSuccess)                                                                   \
+      return fail(PRISMQ_E_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_));           \
+  } while (0)
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// first-fit range allocator over one arena segment
+// ---------------------------------------------------------------------------
+struct RangeAlloc {
+  int64_t cap = 0;
+  std::map<int64_t, int64_t> free_;  // begin -> size
+  void init(int64_t c) {
+    cap = c;
+    free_.clear();
+    if (c > 0) free_[0] = c;
+  }
+  int64_t alloc(int64_t n, int64_t align = 1) {
+    if (n == 0) return 0;
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+      const int64_t b = it->first, sz = it->second;
+      const int64_t ab = (b + align - 1) / align * align;
+      if (ab + n > b + sz) continue;
+      free_.erase(it);
+      if (ab > b) free_[b] = ab - b;
+      if (b + sz > ab + n) free_[ab + n] = b + sz - (ab + n);
+      return ab;
+    }
+    return -1;
+  }
+  void release(int64_t b, int64_t n) {
+    if (n == 0) return;
+    auto it = free_.emplace(b, n).first;
+    auto nx = std::next(it);
+    if (nx != free_.end() && it->first + it->second == nx->first) {
+      it->second += nx->second;
+      free_.erase(nx);
+    }
+    if (it != free_.begin()) {
+      auto pv = std::prev(it);
+      if (pv->first + pv->second == it->first) {
+        pv->second += it->second;
+        free_.erase(it);
+      }
+    }
+  }
+  // one past the highest allocated element
+  int64_t high() const {
+    if (free_.empty()) return cap;
+    auto last = std::prev(free_.end());
+    return last->first + last->second == cap ? last->first : cap;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// lowered (host, system-local indices) form of one topology
+// ---------------------------------------------------------------------------
+struct Lowered {
+  int n = 0;
+  std::vector<float4> pos, vel;
+  std::vector<float2> lj;
+  std::vector<unsigned long long> mask_all, mask_ref;
+  std::vector<int2> far;
+  std::vector<int> far_list;
+  std::vector<Incidence> inc;
+  std::vector<int> inc_list;  // local term index * 4 + position
+  std::vector<int2> ex_idx;
+  std::vector<int> ex_partner;
+  std::vector<float4> ex_par;
+  std::vector<BondT> bonds;
+  std::vector<AngleT> angles;
+  std::vector<DihT> dihs;
+  std::vector<Unit> units;
+  std::vector<float> charges, masses;
+  float ref_origin[3] = {0, 0, 0};
+  int ref_dims[3] = {1, 1, 1};
+  bool ref_ok = false;
+  int cell_cap = 64;
+};
+
+bool finite_pos(float x) { return std::isfinite(x); }
+
+prismq_status lower_topology(const prismq_topology* T, Lowered* L) {
+  if (!T) return fail(PRISMQ_E_INVALID, "topology is NULL");
+  const int n = T->n_atoms;
+  if (n <= 0) return fail(PRISMQ_E_INVALID, "topology has no atoms");
+  if (n > (1 << 29)) return fail(PRISMQ_E_INVALID, "topology exceeds 2^29 atoms");
+  if (!T->positions || !T->masses || !T->charges || !T->lj_sigma || !T->lj_epsilon)
+    return fail(PRISMQ_E_INVALID, "topology per-atom arrays must be non-NULL");
+  L->n = n;
+  L->pos.resize(n);
+  L->vel.resize(n);
+  L->lj.resize(n);
+  L->charges.assign(T->charges, T->charges + n);
+  L->masses.assign(T->masses, T->masses + n);
+  for (int a = 0; a < n; ++a) {
+    const float x = T->positions[3 * a], y = T->positions[3 * a + 1], z = T->positions[3 * a + 2];
+    if (!finite_pos(x) || !finite_pos(y) || !finite_pos(z))
+      return fail(PRISMQ_E_INVALID, "non-finite position at atom " + std::to_string(a));
+    const float m = T->masses[a];
+    if (!(m > 0.0f) || !std::isfinite(m))
+      return fail(PRISMQ_E_INVALID, "mass must be positive and finite at atom " + std::to_string(a));
+    const float sg = T->lj_sigma[a], ep = T->lj_epsilon[a];
+    if (!(sg >= 0.0f) || !(ep >= 0.0f) || !std::isfinite(sg) || !std::isfinite(ep) ||
+        !std::isfinite(T->charges[a]))
+      return fail(PRISMQ_E_INVALID, "invalid charge/LJ parameter at atom " + std::to_string(a));
+    L->pos[a] = make_float4(x, y, z, T->charges[a]);
+    L->vel[a] = make_float4(0.f, 0.f, 0.f, m);
+    L->lj[a] = make_float2(0.5f * sg, sqrtf(ep));
+  }
+  auto in_range = [n](int i) { return i >= 0 && i < n; };
+  // ---- bonded terms + incidence ----
+  std::vector<std::vector<int>> ib(n), ia(n), id(n);
+  for (int t = 0; t < T->n_bonds; ++t) {
+    const prismq_bond& b = T->bonds[t];
+    if (!in_range(b.i) || !in_range(b.j) || b.i == b.j)
+      return fail(PRISMQ_E_INVALID, "bond " + std::to_string(t) + " has invalid atoms");
+    L->bonds.push_back({b.i, b.j, b.r0, b.k});
+    ib[b.i].push_back(t * 4 + 0);
+    ib[b.j].push_back(t * 4 + 1);
+  }
+  for (int t = 0; t < T->n_angles; ++t) {
+    const prismq_angle& g = T->angles[t];
+    if (!in_range(g.i) || !in_range(g.j) || !in_range(g.k) || g.i == g.j || g.j == g.k || g.i == g.k)
+      return fail(PRISMQ_E_INVALID, "angle " + std::to_string(t) + " has invalid atoms");
+    L->angles.push_back({g.i, g.j, g.k, g.theta0, g.force_k});
+    ia[g.i].push_back(t * 4 + 0);
+    ia[g.j].push_back(t * 4 + 1);
+    ia[g.k].push_back(t * 4 + 2);
+  }
+  for (int t = 0; t < T->n_dihedrals; ++t) {
+    const prismq_dihedral& d = T->dihedrals[t];
+    if (!in_range(d.i) || !in_range(d.j) || !in_range(d.k) || !in_range(d.l))
+      return fail(PRISMQ_E_INVALID, "dihedral " + std::to_string(t) + " has invalid atoms");
+    L->dihs.push_back({d.i, d.j, d.k, d.l, d.periodicity, d.phase, d.force_k});
+    id[d.i].push_back(t * 4 + 0);
+    id[d.j].push_back(t * 4 + 1);
+    id[d.k].push_back(t * 4 + 2);
+    id[d.l].push_back(t * 4 + 3);
+  }
+  if ((int64_t)L->bonds.size() >= (1 << 29) || (int64_t)L->angles.size() >= (1 << 29) ||
+      (int64_t)L->dihs.size() >= (1 << 29))
+    return fail(PRISMQ_E_INVALID, "too many bonded terms");
+  L->inc.resize(n);
+  for (int a = 0; a < n; ++a) {
+    if (ib[a].size() > 255 || ia[a].size() > 255 || id[a].size() > 255)
+      return fail(PRISMQ_E_INVALID, "more than 255 terms of one kind on atom " + std::to_string(a));
+    Incidence I;
+    I.b_beg = (int)L->inc_list.size();
+    L->inc_list.insert(L->inc_list.end(), ib[a].begin(), ib[a].end());
+    I.a_beg = (int)L->inc_list.size();
+    L->inc_list.insert(L->inc_list.end(), ia[a].begin(), ia[a].end());
+    I.d_beg = (int)L->inc_list.size();
+    L->inc_list.insert(L->inc_list.end(), id[a].begin(), id[a].end());
+    I.counts = (int)ib[a].size() | ((int)ia[a].size() << 8) | ((int)id[a].size() << 16);
+    L->inc[a] = I;
+  }
+  // ---- exceptions (both directions, ascending partner, last definition wins) ----
+  std::vector<std::map<int, float4>> exc(n);
+  for (int t = 0; t < T->n_exceptions; ++t) {
+    const prismq_exception& e = T->exceptions[t];
+    if (!in_range(e.i) || !in_range(e.j) || e.i == e.j)
+      return fail(PRISMQ_E_INVALID, "exception " + std::to_string(t) + " has invalid atoms");
+    if (!std::isfinite(e.charge_product) || !std::isfinite(e.sigma) || !std::isfinite(e.epsilon))
+      return fail(PRISMQ_E_INVALID, "exception " + std::to_string(t) + " has non-finite parameters");
+    const float4 p = make_float4(e.charge_product, e.sigma, e.epsilon, 0.f);
+    exc[e.i][e.j] = p;
+    exc[e.j][e.i] = p;
+  }
+  L->ex_idx.resize(n);
+  for (int a = 0; a < n; ++a) {
+    L->ex_idx[a] = make_int2((int)L->ex_partner.size(), (int)exc[a].size());
+    for (auto& kv : exc[a]) {
+      L->ex_partner.push_back(kv.first);
+      L->ex_par.push_back(kv.second);
+    }
+  }
+  // ---- exclusion window masks ----
+  L->mask_all.assign(n, 0ull);
+  L->mask_ref.assign(n, 0ull);
+  L->far.assign(n, make_int2(0, 0));
+  if (T->exclusion_offsets) {
+    if (T->exclusion_offsets[0] != 0) return fail(PRISMQ_E_INVALID, "exclusion_offsets[0] must be 0");
+    for (int a = 0; a < n; ++a)
+      if (T->exclusion_offsets[a + 1] < T->exclusion_offsets[a])
+        return fail(PRISMQ_E_INVALID, "exclusion_offsets must be non-decreasing");
+    if (T->exclusion_offsets[n] > 0 && !T->exclusions)
+      return fail(PRISMQ_E_INVALID, "exclusions array is NULL");
+  }
+  for (int a = 0; a < n; ++a) {
+    std::map<int, int> part;  // partner -> is_exception
+    if (T->exclusion_offsets) {
+      for (int q = T->exclusion_offsets[a]; q < T->exclusion_offsets[a + 1]; ++q) {
+        const int j = T->exclusions[q];
+        if (!in_range(j) || j == a)
+          return fail(PRISMQ_E_INVALID, "exclusion partner out of range at atom " + std::to_string(a));
+        part[j] = exc[a].count(j) ? 1 : 0;
+      }
+    }
+    for (auto& kv : exc[a]) part[kv.first] = 1;  // exception pairs never enter ordinary rows
+    const int fb = (int)L->far_list.size();
+    for (auto& kv : part) {
+      const int d = kv.first - a;
+      if (d >= -32 && d < 32) {
+        L->mask_all[a] |= 1ull << (d + 32);
+        if (!kv.second) L->mask_ref[a] |= 1ull << (d + 32);
+      } else {
+        L->far_list.push_back(kv.first | (kv.second ? 0x40000000 : 0));
+      }
+    }
+    L->far[a] = make_int2(fb, (int)L->far_list.size() - fb);
+  }
+  // ---- constraint units (fused_engine.rs:11827-11938) ----
+  std::vector<int> owner(n, -1);
+  for (int c = 0; c < T->n_clusters; ++c) {
+    const prismq_hcluster& h = T->clusters[c];
+    const std::string tag = "SHAKE/RATTLE cluster " + std::to_string(c) + ": ";
+    if (!in_range(h.central_atom)) return fail(PRISMQ_E_INVALID, tag + "central atom out of range");
+    if (h.n_hydrogens < 1 || h.n_hydrogens > 3) return fail(PRISMQ_E_INVALID, tag + "n_hydrogens must be 1..3");
+    if (!(h.inv_mass_central > 0.f) || !std::isfinite(h.inv_mass_central) || !(h.inv_mass_h > 0.f) ||
+        !std::isfinite(h.inv_mass_h))
+      return fail(PRISMQ_E_INVALID, tag + "invalid inverse masses");
+    const double live_c = 1.0 / (double)T->masses[h.central_atom];
+    if (std::fabs((double)h.inv_mass_central - live_c) / std::max(live_c, 2.2e-16) > 1.0e-6)
+      return fail(PRISMQ_E_INVALID, tag + "central inverse mass disagrees with the atom mass");
+    if (owner[h.central_atom] >= 0) return fail(PRISMQ_E_INVALID, tag + "clusters overlap");
+    owner[h.central_atom] = c;
+    Unit U;
+    std::memset(&U, 0, sizeof(U));
+    U.a[0] = h.central_atom;
+    U.a[1] = U.a[2] = U.a[3] = -1;
+    U.nh = h.n_hydrogens;
+    U.inv_mc = h.inv_mass_central;
+    U.inv_mh = h.inv_mass_h;
+    for (int q = 0; q < h.n_hydrogens; ++q) {
+      const int hq = h.hydrogen_atoms[q];
+      if (!in_range(hq) || hq == h.central_atom) return fail(PRISMQ_E_INVALID, tag + "invalid hydrogen atom");
+      const float L0 = h.bond_lengths[q];
+      if (!(L0 > 0.f) || !std::isfinite(L0)) return fail(PRISMQ_E_INVALID, tag + "invalid bond length");
+      const double live_h = 1.0 / (double)T->masses[hq];
+      if (std::fabs((double)h.inv_mass_h - live_h) / std::max(live_h, 2.2e-16) > 1.0e-6)
+        return fail(PRISMQ_E_INVALID, tag + "hydrogen inverse mass disagrees with the atom mass");
+      if (owner[hq] >= 0) return fail(PRISMQ_E_INVALID, tag + "clusters overlap");
+      owner[hq] = c;
+      U.a[1 + q] = hq;
+      U.r0[q] = L0;
+    }
+    L->units.push_back(U);
+  }
+  for (int a = 0; a < n; ++a)
+    if (owner[a] < 0) {
+      Unit U;
+      std::memset(&U, 0, sizeof(U));
+      U.a[0] = a;
+      U.a[1] = U.a[2] = U.a[3] = -1;
+      U.nh = 0;
+      L->units.push_back(U);
+    }
+  std::stable_sort(L->units.begin(), L->units.end(), [](const Unit& x, const Unit& y) { return x.a[0] < y.a[0]; });
+  // ---- reference grid (CELL_SIZE 10 Å, one cell of padding, ≤ 32 per axis) ----
+  float mn[3] = {3.4e38f, 3.4e38f, 3.4e38f}, mx[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
+  for (int a = 0; a < n; ++a)
+    for (int d = 0; d < 3; ++d) {
+      mn[d] = std::min(mn[d], T->positions[3 * a + d]);
+      mx[d] = std::max(mx[d], T->positions[3 * a + d]);
+    }
+  L->ref_ok = true;
+  long long ref_cells = 1;
+  for (int d = 0; d < 3; ++d) {
+    L->ref_origin[d] = mn[d] - 10.0f;
+    const float extent = (mx[d] - mn[d]) + 2.0f * 10.0f;
+    long long v = (long long)std::ceil(extent / 10.0f);
+    if (v < 1) v = 1;
+    if (v > kRefMaxDim) L->ref_ok = false;
+    L->ref_dims[d] = (int)std::min<long long>(v, kRefMaxDim);
+    ref_cells *= L->ref_dims[d];
+  }
+  L->cell_cap = (int)std::max<long long>({64LL, (long long)n / 32, L->ref_ok ? ref_cells : 0LL});
+  return PRISMQ_OK;
+}
+
+// Maxwell–Boltzmann velocities: σ_v = sqrt(418.4·k_B·T/m), COM removed.
+void init_velocities(Lowered* L, const prismq_params& p) {
+  const int n = L->n;
+  std::vector<double> vx(n), vy(n), vz(n);
+  double px = 0, py = 0, pz = 0, M = 0;
+  for (int a = 0; a < n; ++a) {
+    const float m = L->vel[a].w;
+    float z0 = 0.f, z1 = 0.f, z2 = 0.f;
+    if (p.temperature > 0.f) normal3(p.seed, p.stream, (uint32_t)a, 0xffffffffffffull, 3u, &z0, &z1, &z2);
+    const float sg = sqrtf(kKcalToAmuA2Ps2 * kBoltzmann * p.temperature / m);
+    vx[a] = sg * z0;
+    vy[a] = sg * z1;
+    vz[a] = sg * z2;
+    px += m * vx[a];
+    py += m * vy[a];
+    pz += m * vz[a];
+    M += m;
+  }
+  for (int a = 0; a < n; ++a) {
+    L->vel[a].x = (float)(vx[a] - px / M);
+    L->vel[a].y = (float)(vy[a] - py / M);
+    L->vel[a].z = (float)(vz[a] - pz / M);
+  }
+}
+
+prismq_status check_params(const prismq_params* p) {
+  if (!p) return fail(PRISMQ_E_INVALID, "params is NULL");
+  if (!(p->dt > 0.f) || !std::isfinite(p->dt)) return fail(PRISMQ_E_INVALID, "dt must be positive");
+  if (!(p->temperature >= 0.f) || !std::isfinite(p->temperature))
+    return fail(PRISMQ_E_INVALID, "temperature must be >= 0");
+  if (!(p->gamma >= 0.f) || !std::isfinite(p->gamma)) return fail(PRISMQ_E_INVALID, "gamma must be >= 0");
+  if (!(p->cutoff > 0.f) || !(p->skin >= 0.f)) return fail(PRISMQ_E_INVALID, "cutoff/skin invalid");
+  if (p->rebuild_interval < 1) return fail(PRISMQ_E_INVALID, "rebuild_interval must be >= 1");
+  if (p->max_constraint_iter < 1) return fail(PRISMQ_E_INVALID, "max_constraint_iter must be >= 1");
+  if (p->com_interval < 0) return fail(PRISMQ_E_INVALID, "com_interval must be >= 0");
+  return PRISMQ_OK;
+}
+
+void fill_params(SysDev* S, const prismq_params& p) {
+  S->dt = p.dt;
+  S->temperature = p.temperature;
+  S->gamma = p.gamma;
+  const float hd = 0.5f * p.dt;
+  const float arg = -p.gamma * hd;
+  S->c1 = (float)std::exp((double)arg);  // exp(-γ·dt/2), rounded once to float
+  const float rl = p.cutoff + p.skin;
+  S->rlist2 = rl * rl;
+  S->half_skin2 = (0.5f * p.skin) * (0.5f * p.skin);
+  S->ref_r2 = (p.cutoff * p.cutoff) * 1.44f;
+  S->cut2 = p.cutoff * p.cutoff;
+  S->rebuild_interval = p.rebuild_interval;
+  S->com_interval = p.com_interval;
+  S->max_iter = p.max_constraint_iter;
+  S->seed = p.seed;
+  S->stream = p.stream;
+}
+
+// ---------------------------------------------------------------------------
+// small transfer kernels (AoS float[3N] <-> SoA float4 streams)
+// ---------------------------------------------------------------------------
+__global__ void k_aos_to_xyz(float4* dst, const float* src, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 o = dst[i];
+  dst[i] = make_float4(src[3 * i], src[3 * i + 1], src[3 * i + 2], o.w);
+}
+__global__ void k_xyz_to_aos(float* dst, const float4* src, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 v = src[i];
+  dst[3 * i] = v.x;
+  dst[3 * i + 1] = v.y;
+  dst[3 * i + 2] = v.z;
+}
+__global__ void k_fill_int(int* p, int v, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = v;
+}
+__global__ void k_deactivate_units(Unit* u, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) u[i].nh = -1;
+}
+
+struct SlotRec {
+  bool active = false;
+  int64_t atom_b = 0, n_atoms = 0, unit_b = 0, n_units = 0;
+  int64_t bond_b = 0, n_bonds = 0, angle_b = 0, n_angles = 0, dih_b = 0, n_dihs = 0;
+  int64_t inc_b = 0, n_inc = 0, ex_b = 0, n_ex = 0, far_b = 0, n_far = 0, cell_b = 0, n_cell = 0;
+  bool ref_ok = false;
+  bool need_prime = true;
+  prismq_params params{};
+};
+
+}  // namespace
+
+struct prismq_batch {
+  Arena A;
+  RangeAlloc r_atoms, r_units, r_bonds, r_angles, r_dihs, r_inc, r_ex, r_far, r_cells;
+  std::vector<SlotRec> slots;
+  cudaStream_t st = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  bool graph_dirty = true;
+  int64_t atom_span = 0, unit_span = 0;
+  int sys_span = 0;
+  double* d_energy = nullptr;
+  float* d_stage = nullptr;
+  std::vector<SysDev> h_sys;
+
+  ~prismq_batch() {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    void* ptrs[] = {A.pos, A.vel, A.lj, A.xref, A.f, A.pe, A.atom_sys, A.mask_all, A.mask_ref, A.far,
+                    A.far_list, A.inc, A.inc_list, A.ex_idx, A.ex_partner, A.ex_par, A.bonds, A.angles,
+                    A.dihs, A.units, A.nbr, A.nnbr, A.cell_start, A.cell_atoms, A.atom_cell, A.sys,
+                    d_energy, d_stage};
+    for (void* p : ptrs)
+      if (p) cudaFree(p);
+    if (st) cudaStreamDestroy(st);
+  }
+
+  void update_spans() {
+    const int64_t na = r_atoms.high(), nu = r_units.high();
+    int ns = 0;
+    for (int i = 0; i < (int)slots.size(); ++i)
+      if (slots[i].active) ns = i + 1;
+    if (na != atom_span || nu != unit_span || ns != sys_span) graph_dirty = true;
+    atom_span = na;
+    unit_span = nu;
+    sys_span = ns;
+  }
+
+  prismq_status sync_sys_from_device() {
+    if (sys_span == 0) return PRISMQ_OK;
+    PQ_CK(cudaMemcpyAsync(h_sys.data(), A.sys, sizeof(SysDev) * sys_span, cudaMemcpyDeviceToHost, st));
+    PQ_CK(cudaStreamSynchronize(st));
+    return PRISMQ_OK;
+  }
+
+  void enqueue_step_body() {
+    launch_control_cells(A, sys_span, kCtlStep, -1, st);
+    launch_nbr_build(A, atom_span, 1, st);
+    launch_force(A, atom_span, false, st);
+  }
+
+  prismq_status ensure_graph() {
+    if (!graph_dirty && gexec) return PRISMQ_OK;
+    if (gexec) {
+      cudaGraphExecDestroy(gexec);
+      gexec = nullptr;
+    }
+    cudaGraph_t g;
+    PQ_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    enqueue_step_body();
+    launch_integrate(A, unit_span, kIntBoth, st);
+    PQ_CK(cudaStreamEndCapture(st, &g));
+    cudaError_t e = cudaGraphInstantiate(&gexec, g, 0);
+    cudaGraphDestroy(g);
+    PQ_CK(e);
+    graph_dirty = false;
+    return PRISMQ_OK;
+  }
+
+  prismq_status prime_if_needed() {
+    bool any = false;
+    for (auto& s : slots)
+      if (s.active && s.need_prime) any = true;
+    if (!any) return PRISMQ_OK;
+    launch_control_cells(A, sys_span, kCtlPrime, -1, st);
+    launch_nbr_build(A, atom_span, 1, st);
+    launch_force(A, atom_span, false, st);
+    g_launches += 3;
+    PQ_CK(cudaGetLastError());
+    for (auto& s : slots) s.need_prime = false;
+    return PRISMQ_OK;
+  }
+
+  prismq_status check_status(int only_slot = -1) {
+    prismq_status rc = sync_sys_from_device();
+    if (rc != PRISMQ_OK) return rc;
+    for (int i = 0; i < sys_span; ++i) {
+      if (!slots[i].active) continue;
+      if (only_slot >= 0 && i != only_slot) continue;
+      const int stt = h_sys[i].status;
+      if (stt) return status_error(stt, i);
+    }
+    return PRISMQ_OK;
+  }
+
+  static prismq_status status_error(int stt, int slot) {
+    const std::string where = " (system slot " + std::to_string(slot) + ")";
+    if (stt & kStShake) return fail(PRISMQ_E_SHAKE, "SHAKE did not converge" + where);
+    if (stt & kStRattle) return fail(PRISMQ_E_RATTLE, "RATTLE did not converge" + where);
+    if (stt & kStCellOverflow) return fail(PRISMQ_E_CELL_OVERFLOW, "cell occupancy above 512" + where);
+    if (stt & kStNbrOverflow) return fail(PRISMQ_E_NEIGHBOR_OVERFLOW, "neighbour row above 1024" + where);
+    return fail(PRISMQ_E_NONFINITE, "non-finite state" + where);
+  }
+
+  prismq_status step(int64_t n) {
+    if (n <= 0) return PRISMQ_OK;
+    if (sys_span == 0) return PRISMQ_OK;
+    prismq_status rc = prime_if_needed();
+    if (rc != PRISMQ_OK) return rc;
+    rc = ensure_graph();
+    if (rc != PRISMQ_OK) return rc;
+    launch_integrate(A, unit_span, kIntPre, st);
+    g_launches += 1;
+    for (int64_t i = 1; i < n; ++i) {
+      PQ_CK(cudaGraphLaunch(gexec, st));
+      g_launches += 4;
+    }
+    enqueue_step_body();
+    launch_integrate(A, unit_span, kIntPost, st);
+    g_launches += 4;
+    PQ_CK(cudaGetLastError());
+    return check_status();
+  }
+};
+
+struct prismq_system {
+  prismq_batch* b = nullptr;
+  int slot = 0;
+};
+
+namespace {
+
+prismq_status batch_alloc(prismq_batch* B, int64_t atom_cap, int sys_cap, int64_t bond_cap,
+                          int64_t angle_cap, int64_t dih_cap, int64_t inc_cap, int64_t ex_cap,
+                          int64_t far_cap, int64_t cell_cap) {
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return fail(PRISMQ_E_NO_DEVICE, "no CUDA device visible");
+  }
+  atom_cap = (atom_cap + 31) / 32 * 32;
+  Arena& A = B->A;
+  A.atom_cap = atom_cap;
+  A.unit_cap = atom_cap;
+  A.bond_cap = std::max<int64_t>(bond_cap, 1);
+  A.angle_cap = std::max<int64_t>(angle_cap, 1);
+  A.dih_cap = std::max<int64_t>(dih_cap, 1);
+  A.inc_cap = std::max<int64_t>(inc_cap, 1);
+  A.ex_cap = std::max<int64_t>(ex_cap, 1);
+  A.far_cap = std::max<int64_t>(far_cap, 1);
+  A.cell_cap = std::max<int64_t>(cell_cap, 1);
+  A.sys_cap = sys_cap;
+  PQ_CK(cudaStreamCreateWithFlags(&B->st, cudaStreamNonBlocking));
+#define PQ_ALLOC(ptr, count) PQ_CK(cudaMalloc((void**)&(ptr), sizeof(*(ptr)) * (size_t)(count)))
+  PQ_ALLOC(A.pos, atom_cap);
+  PQ_ALLOC(A.vel, atom_cap);
+  PQ_ALLOC(A.lj, atom_cap);
+  PQ_ALLOC(A.xref, atom_cap);
+  PQ_ALLOC(A.f, 3 * atom_cap);
+  PQ_ALLOC(A.pe, 5 * atom_cap);
+  PQ_ALLOC(A.atom_sys, atom_cap);
+  PQ_ALLOC(A.mask_all, atom_cap);
+  PQ_ALLOC(A.mask_ref, atom_cap);
+  PQ_ALLOC(A.far, atom_cap);
+  PQ_ALLOC(A.far_list, A.far_cap);
+  PQ_ALLOC(A.inc, atom_cap);
+  PQ_ALLOC(A.inc_list, A.inc_cap);
+  PQ_ALLOC(A.ex_idx, atom_cap);
+  PQ_ALLOC(A.ex_partner, A.ex_cap);
+  PQ_ALLOC(A.ex_par, A.ex_cap);
+  PQ_ALLOC(A.bonds, A.bond_cap);
+  PQ_ALLOC(A.angles, A.angle_cap);
+  PQ_ALLOC(A.dihs, A.dih_cap);
+  PQ_ALLOC(A.units, A.unit_cap);
+  PQ_ALLOC(A.nbr, (atom_cap / 32) * (int64_t)kNbrCap * 32);
+  PQ_ALLOC(A.nnbr, atom_cap);
+  PQ_ALLOC(A.cell_start, A.cell_cap);
+  PQ_ALLOC(A.cell_atoms, atom_cap);
+  PQ_ALLOC(A.atom_cell, atom_cap);
+  PQ_ALLOC(A.sys, sys_cap);
+  PQ_ALLOC(B->d_energy, 6 * (int64_t)sys_cap);
+  PQ_ALLOC(B->d_stage, 3 * atom_cap);
+#undef PQ_ALLOC
+  PQ_CK(cudaMemsetAsync(A.sys, 0, sizeof(SysDev) * sys_cap, B->st));
+  PQ_CK(cudaMemsetAsync(A.nnbr, 0, sizeof(int) * atom_cap, B->st));
+  PQ_CK(cudaMemsetAsync(A.f, 0, sizeof(long long) * 3 * atom_cap, B->st));
+  PQ_CK(cudaMemsetAsync(A.pe, 0, sizeof(double) * 5 * atom_cap, B->st));
+  k_fill_int<<<(unsigned)((atom_cap + 255) / 256), 256, 0, B->st>>>(A.atom_sys, -1, atom_cap);
+  k_deactivate_units<<<(unsigned)((atom_cap + 255) / 256), 256, 0, B->st>>>(A.units, atom_cap);
+  PQ_CK(cudaGetLastError());
+  PQ_CK(cudaStreamSynchronize(B->st));
+  B->r_atoms.init(atom_cap);
+  B->r_units.init(atom_cap);
+  B->r_bonds.init(A.bond_cap);
+  B->r_angles.init(A.angle_cap);
+  B->r_dihs.init(A.dih_cap);
+  B->r_inc.init(A.inc_cap);
+  B->r_ex.init(A.ex_cap);
+  B->r_far.init(A.far_cap);
+  B->r_cells.init(A.cell_cap);
+  B->slots.resize(sys_cap);
+  B->h_sys.resize(sys_cap);
+  return PRISMQ_OK;
+}
+
+template <class T>
+prismq_status upload(T* dst, const std::vector<T>& src, cudaStream_t st) {
+  if (src.empty()) return PRISMQ_OK;
+  PQ_CK(cudaMemcpyAsync(dst, src.data(), sizeof(T) * src.size(), cudaMemcpyHostToDevice, st));
+  return PRISMQ_OK;
+}
+
+prismq_status batch_admit(prismq_batch* B, const Lowered& L0, const prismq_params& p, int* slot_out) {
+  int slot = -1;
+  for (int i = 0; i < (int)B->slots.size(); ++i)
+    if (!B->slots[i].active) {
+      slot = i;
+      break;
+    }
+  if (slot < 0) return fail(PRISMQ_E_CAPACITY, "batch has no free system slot");
+  Lowered L = L0;
+  SlotRec R;
+  R.n_atoms = L.n;
+  R.n_units = (int64_t)L.units.size();
+  R.n_bonds = (int64_t)L.bonds.size();
+  R.n_angles = (int64_t)L.angles.size();
+  R.n_dihs = (int64_t)L.dihs.size();
+  R.n_inc = (int64_t)L.inc_list.size();
+  R.n_ex = (int64_t)L.ex_partner.size();
+  R.n_far = (int64_t)L.far_list.size();
+  R.n_cell = 2 * ((int64_t)L.cell_cap + 1);
+  struct Req {
+    RangeAlloc* r;
+    int64_t n;
+    int64_t* b;
+    int64_t align;
+  } reqs[] = {{&B->r_atoms, R.n_atoms, &R.atom_b, 32}, {&B->r_units, R.n_units, &R.unit_b, 1},
+              {&B->r_bonds, R.n_bonds, &R.bond_b, 1},  {&B->r_angles, R.n_angles, &R.angle_b, 1},
+              {&B->r_dihs, R.n_dihs, &R.dih_b, 1},     {&B->r_inc, R.n_inc, &R.inc_b, 1},
+              {&B->r_ex, R.n_ex, &R.ex_b, 1},          {&B->r_far, R.n_far, &R.far_b, 1},
+              {&B->r_cells, R.n_cell, &R.cell_b, 1}};
+  int done = 0;
+  for (auto& q : reqs) {
+    const int64_t b = q.r->alloc(q.n, q.align);
+    if (b < 0) {
+      for (int k = 0; k < done; ++k) reqs[k].r->release(*reqs[k].b, reqs[k].n);
+      return fail(PRISMQ_E_CAPACITY, "batch arena has no room for this system");
+    }
+    *q.b = b;
+    ++done;
+  }
+  const int ab = (int)R.atom_b;
+  // globalise indices
+  for (auto& b : L.bonds) {
+    b.i += ab;
+    b.j += ab;
+  }
+  for (auto& g : L.angles) {
+    g.i += ab;
+    g.j += ab;
+    g.k += ab;
+  }
+  for (auto& d : L.dihs) {
+    d.i += ab;
+    d.j += ab;
+    d.k += ab;
+    d.l += ab;
+  }
+  for (int a = 0; a < L.n; ++a) {
+    Incidence& I = L.inc[a];
+    const int nb = I.counts & 0xff, na = (I.counts >> 8) & 0xff, nd = (I.counts >> 16) & 0xff;
+    for (int q = 0; q < nb; ++q) L.inc_list[I.b_beg + q] += (int)R.bond_b * 4;
+    for (int q = 0; q < na; ++q) L.inc_list[I.a_beg + q] += (int)R.angle_b * 4;
+    for (int q = 0; q < nd; ++q) L.inc_list[I.d_beg + q] += (int)R.dih_b * 4;
+    I.b_beg += (int)R.inc_b;
+    I.a_beg += (int)R.inc_b;
+    I.d_beg += (int)R.inc_b;
+    L.ex_idx[a].x += (int)R.ex_b;
+    L.far[a].x += (int)R.far_b;
+  }
+  for (auto& j : L.ex_partner) j += ab;
+  for (auto& e : L.far_list) e = ((e & 0x3fffffff) + ab) | (e & 0x40000000);
+  for (auto& U : L.units) {
+    for (int k = 0; k < 4; ++k)
+      if (U.a[k] >= 0) U.a[k] += ab;
+    U.sys = slot;
+  }
+  std::vector<int> asys(L.n, slot);
+  cudaStream_t st = B->st;
+  Arena& A = B->A;
+  prismq_status rc;
+#define PQ_UP(dst, vec) \
+  if ((rc = upload((dst), (vec), st)) != PRISMQ_OK) return rc;
+  PQ_UP(A.pos + ab, L.pos);
+  PQ_UP(A.vel + ab, L.vel);
+  PQ_UP(A.xref + ab, L.pos);
+  PQ_UP(A.lj + ab, L.lj);
+  PQ_UP(A.atom_sys + ab, asys);
+  PQ_UP(A.mask_all + ab, L.mask_all);
+  PQ_UP(A.mask_ref + ab, L.mask_ref);
+  PQ_UP(A.far + ab, L.far);
+  PQ_UP(A.far_list + R.far_b, L.far_list);
+  PQ_UP(A.inc + ab, L.inc);
+  PQ_UP(A.inc_list + R.inc_b, L.inc_list);
+  PQ_UP(A.ex_idx + ab, L.ex_idx);
+  PQ_UP(A.ex_partner + R.ex_b, L.ex_partner);
+  PQ_UP(A.ex_par + R.ex_b, L.ex_par);
+  PQ_UP(A.bonds + R.bond_b, L.bonds);
+  PQ_UP(A.angles + R.angle_b, L.angles);
+  PQ_UP(A.dihs + R.dih_b, L.dihs);
+  PQ_UP(A.units + R.unit_b, L.units);
+#undef PQ_UP
+  PQ_CK(cudaMemsetAsync(A.nnbr + ab, 0, sizeof(int) * L.n, st));
+  PQ_CK(cudaMemsetAsync(A.f + ab, 0, sizeof(long long) * L.n, st));
+  PQ_CK(cudaMemsetAsync(A.f + A.atom_cap + ab, 0, sizeof(long long) * L.n, st));
+  PQ_CK(cudaMemsetAsync(A.f + 2 * A.atom_cap + ab, 0, sizeof(long long) * L.n, st));
+  SysDev S;
+  std::memset(&S, 0, sizeof(S));
+  S.atom_begin = ab;
+  S.n_atoms = L.n;
+  S.unit_begin = (int)R.unit_b;
+  S.n_units = (int)R.n_units;
+  S.cell_begin = (int)R.cell_b;
+  S.cell_cap = L.cell_cap;
+  S.active = 1;
+  S.nbr_mode = 0;
+  fill_params(&S, p);
+  for (int d = 0; d < 3; ++d) {
+    S.ref_origin[d] = L.ref_origin[d];
+    S.ref_dims[d] = L.ref_dims[d];
+  }
+  S.need_prime = 1;
+  PQ_CK(cudaMemcpyAsync(A.sys + slot, &S, sizeof(S), cudaMemcpyHostToDevice, st));
+  PQ_CK(cudaStreamSynchronize(st));
+  R.active = true;
+  R.ref_ok = L.ref_ok;
+  R.need_prime = true;
+  R.params = p;
+  B->slots[slot] = R;
+  B->h_sys[slot] = S;
+  B->update_spans();
+  *slot_out = slot;
+  return PRISMQ_OK;
+}
+
+prismq_status batch_release(prismq_batch* B, int slot) {
+  if (slot < 0 || slot >= (int)B->slots.size() || !B->slots[slot].active)
+    return fail(PRISMQ_E_NOT_FOUND, "no resident system in slot " + std::to_string(slot));
+  SlotRec& R = B->slots[slot];
+  Arena& A = B->A;
+  cudaStream_t st = B->st;
+  PQ_CK(cudaMemsetAsync(A.atom_sys + R.atom_b, 0xff, sizeof(int) * R.n_atoms, st));
+  if (R.n_units)
+    k_deactivate_units<<<(unsigned)((R.n_units + 255) / 256), 256, 0, st>>>(A.units + R.unit_b, R.n_units);
+  PQ_CK(cudaMemsetAsync(A.sys + slot, 0, sizeof(SysDev), st));
+  PQ_CK(cudaStreamSynchronize(st));
+  B->r_atoms.release(R.atom_b, R.n_atoms);
+  B->r_units.release(R.unit_b, R.n_units);
+  B->r_bonds.release(R.bond_b, R.n_bonds);
+  B->r_angles.release(R.angle_b, R.n_angles);
+  B->r_dihs.release(R.dih_b, R.n_dihs);
+  B->r_inc.release(R.inc_b, R.n_inc);
+  B->r_ex.release(R.ex_b, R.n_ex);
+  B->r_far.release(R.far_b, R.n_far);
+  B->r_cells.release(R.cell_b, R.n_cell);
+  R = SlotRec();
+  B->update_spans();
+  return PRISMQ_OK;
+}
+
+prismq_status get_xyz(prismq_batch* B, int slot, float4* src_plane, float* out) {
+  const SlotRec& R = B->slots[slot];
+  const int n = (int)R.n_atoms;
+  k_xyz_to_aos<<<(n + 255) / 256, 256, 0, B->st>>>(B->d_stage, src_plane + R.atom_b, n);
+  PQ_CK(cudaGetLastError());
+  PQ_CK(cudaMemcpyAsync(out, B->d_stage, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, B->st));
+  PQ_CK(cudaStreamSynchronize(B->st));
+  return PRISMQ_OK;
+}
+
+prismq_status set_xyz(prismq_batch* B, int slot, float4* dst_plane, const float* in) {
+  const SlotRec& R = B->slots[slot];
+  const int n = (int)R.n_atoms;
+  for (int i = 0; i < 3 * n; ++i)
+    if (!std::isfinite(in[i])) return fail(PRISMQ_E_INVALID, "non-finite input value");
+  PQ_CK(cudaMemcpyAsync(B->d_stage, in, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, B->st));
+  k_aos_to_xyz<<<(n + 255) / 256, 256, 0, B->st>>>(dst_plane + R.atom_b, B->d_stage, n);
+  PQ_CK(cudaGetLastError());
+  PQ_CK(cudaStreamSynchronize(B->st));
+  return PRISMQ_OK;
+}
+
+prismq_status mark_prime(prismq_batch* B, int slot) {
+  B->slots[slot].need_prime = true;
+  const int one = 1;
+  PQ_CK(cudaMemcpyAsync(&B->A.sys[slot].need_prime, &one, sizeof(int), cudaMemcpyHostToDevice, B->st));
+  PQ_CK(cudaStreamSynchronize(B->st));
+  return PRISMQ_OK;
+}
+
+prismq_status check_slot(prismq_batch* B, int slot) {
+  if (!B) return fail(PRISMQ_E_INVALID, "batch is NULL");
+  if (slot < 0 || slot >= (int)B->slots.size() || !B->slots[slot].active)
+    return fail(PRISMQ_E_NOT_FOUND, "no resident system in slot " + std::to_string(slot));
+  return PRISMQ_OK;
+}
+
+// Forces + per-atom energy planes at the current positions; returns the
+// system's energy totals in out6 (host) when non-NULL.
+prismq_status eval_energy(prismq_batch* B, int slot, double* out6) {
+  prismq_status rc = B->prime_if_needed();
+  if (rc != PRISMQ_OK) return rc;
+  launch_force(B->A, B->atom_span, true, B->st);
+  launch_energy_reduce(B->A, B->sys_span, B->d_energy, B->st);
+  // the stepping kernels consume forces from the force-only variant
+  launch_force(B->A, B->atom_span, false, B->st);
+  g_launches += 3;
+  PQ_CK(cudaGetLastError());
+  if (out6) {
+    PQ_CK(cudaMemcpyAsync(out6, B->d_energy + 6 * slot, sizeof(double) * 6, cudaMemcpyDeviceToHost, B->st));
+  }
+  PQ_CK(cudaStreamSynchronize(B->st));
+  return B->check_status(slot);
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+const char* prismq_last_error(void) { return g_err.c_str(); }
+int prismq_abi_version(void) { return PRISMQ_ABI_VERSION; }
+int prismq_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+long long prismq_kernel_launches(void) { return g_launches.load(); }
+
+void prismq_params_default(prismq_params* p) {
+  if (!p) return;
+  p->dt = 0.004f;
+  p->temperature = 300.0f;
+  p->gamma = 1.0f;
+  p->cutoff = 10.0f;
+  p->skin = 2.0f;
+  p->rebuild_interval = 20;
+  p->com_interval = 100;
+  p->max_constraint_iter = 100;
+  p->seed = 0x50524953u;
+  p->stream = 0u;
+}
+
+void prismq_debug_noise(uint32_t seed, uint32_t stream, uint32_t atom, uint64_t step, uint32_t purpose,
+                        float out3[3]) {
+  normal3(seed, stream, atom, step, purpose, &out3[0], &out3[1], &out3[2]);
+}
+
+prismq_status prismq_polyala_build(int32_t n_chains, int32_t n_residues, uint64_t seed, float density,
+                                   float box_edge, prismq_topology_buf** out) {
+  if (!out) return fail(PRISMQ_E_INVALID, "out is NULL");
+  auto* b = new prismq_topology_buf();
+  std::string err;
+  if (!polyala_build(n_chains, n_residues, seed, density, box_edge, &b->topo, &err)) {
+    delete b;
+    return fail(PRISMQ_E_INVALID, err);
+  }
+  *out = b;
+  return PRISMQ_OK;
+}
+
+prismq_status prismq_topology_view(const prismq_topology_buf* buf, prismq_topology* out) {
+  if (!buf || !out) return fail(PRISMQ_E_INVALID, "NULL argument");
+  buf->topo.view(out);
+  return PRISMQ_OK;
+}
+
+void prismq_topology_free(prismq_topology_buf* buf) { delete buf; }
+
+// ---- batch ----
+
+prismq_status prismq_batch_create(int64_t max_atoms, int32_t max_systems, prismq_batch** out) {
+  if (!out || max_atoms <= 0 || max_systems <= 0) return fail(PRISMQ_E_INVALID, "invalid batch size");
+  auto* B = new prismq_batch();
+  const int64_t na = (max_atoms + 31) / 32 * 32 + 32 * (int64_t)max_systems;
+  prismq_status rc = batch_alloc(B, na, max_systems, 2 * na, 4 * na, 8 * na, 48 * na, 8 * na, 2 * na,
+                                 2 * (na / 8 + 130 * (int64_t)max_systems));
+  if (rc != PRISMQ_OK) {
+    delete B;
+    return rc;
+  }
+  *out = B;
+  return PRISMQ_OK;
+}
+
+void prismq_batch_destroy(prismq_batch* b) { delete b; }
+
+prismq_status prismq_batch_add_system(prismq_batch* b, const prismq_topology* topo,
+                                      const prismq_params* params, int32_t* slot) {
+  if (!b || !slot) return fail(PRISMQ_E_INVALID, "NULL argument");
+  prismq_status rc = check_params(params);
+  if (rc != PRISMQ_OK) return rc;
+  Lowered L;
+  rc = lower_topology(topo, &L);
+  if (rc != PRISMQ_OK) return rc;
+  init_velocities(&L, *params);
+  int s = -1;
+  rc = batch_admit(b, L, *params, &s);
+  if (rc != PRISMQ_OK) return rc;
+  *slot = s;
+  return PRISMQ_OK;
+}
+
+prismq_status prismq_batch_remove_system(prismq_batch* b, int32_t slot) {
+  if (!b) return fail(PRISMQ_E_INVALID, "batch is NULL");
+  return batch_release(b, slot);
+}
+
+prismq_status prismq_batch_step(prismq_batch* b, int64_t n_steps) {
+  if (!b) return fail(PRISMQ_E_INVALID, "batch is NULL");
+  return b->step(n_steps);
+}
+
+prismq_status prismq_batch_get_state(prismq_batch* b, int32_t slot, float* xyz, float* vxyz) {
+  prismq_status rc = check_slot(b, slot);
+  if (rc != PRISMQ_OK) return rc;
+  if (xyz && (rc = get_xyz(b, slot, b->A.pos, xyz)) != PRISMQ_OK) return rc;
+  if (vxyz && (rc = get_xyz(b, slot, b->A.vel, vxyz)) != PRISMQ_OK) return rc;
+  return PRISMQ_OK;
+}
+
+prismq_status prismq_batch_set_state(prismq_batch* b, int32_t slot, const float* xyz, const float* vxyz) {
+  prismq_status rc = check_slot(b, slot);
+  if (rc != PRISMQ_OK) return rc;
+  if (xyz) {
+    if ((rc = set_xyz(b, slot, b->A.pos, xyz)) != PRISMQ_OK) return rc;
+    if ((rc = mark_prime(b, slot)) != PRISMQ_OK) return rc;
+  }
+  if (vxyz && (rc = set_xyz(b, slot, b->A.vel, vxyz)) != PRISMQ_OK) return rc;
+  return PRISMQ_OK;
+}
+
+prismq_status prismq_batch_get_step(prismq_batch* b, int32_t slot, int64_t* step) {
+  prismq_status rc = check_slot(b, slot);
+  if (rc != PRISMQ_OK) return rc;
+  if (!step) return fail(PRISMQ_E_INVALID, "step is NULL");
+  rc = b->sync_sys_from_device();
+  if (rc != PRISMQ_OK) return rc;
+  *step = b->h_sys[slot].step;
+  return PRISMQ_OK;
+}
+
+prismq_status prismq_batch_status(prismq_batch* b, int32_t slot) {
+  prismq_status rc = check_slot(b, slot);
+  if (rc != PRISMQ_OK) return rc;
+  return b->check_status(slot);
+}
+
+prismq_status prismq_batch_energy(prismq_batch* b, int32_t slot, double out[6]) {
+  prismq_status rc = check_slot(b, slot);
+  if (rc != PRISMQ_OK) return rc;
+  double e[6];
+  rc = eval_energy(b, slot, e);
+  if (rc != PRISMQ_OK) return rc;
+  // five potential planes in order: bond, angle, dihedral, exception, nonbonded; then kinetic
+  for (int i = 0; i < 6; ++i) out[i] = e[i];
+  return PRISMQ_OK;
+}
+
+int64_t prismq_batch_resident_atoms(const prismq_batch* b) {
+  if (!b) return 0;
+  int64_t n = 0;
+  for (auto& s : b->slots)
+    if (s.active) n += s.n_atoms;
+  return n;
+}
+
+int32_t prismq_batch_resident_systems(const prismq_batch* b) {
+  if (!b) return 0;
+  int32_t n = 0;
+  for (auto& s : b->slots)
+    if (s.active) ++n;
+  return n;
+}
+
+// ---- single system ----
+
+prismq_status prismq_system_create(const prismq_topology* topo, const prismq_params* params,
+                                   prismq_system** out) {
+  if (!out) return fail(PRISMQ_E_INVALID, "out is NULL");
+  prismq_status rc = check_params(params);
+  if (rc != PRISMQ_OK) return rc;
+  Lowered L;
+  rc = lower_topology(topo, &L);
+  if (rc != PRISMQ_OK) return rc;
+  init_velocities(&L, *params);
+  auto* B = new prismq_batch();
+  const int64_t n = L.n;
+  rc = batch_alloc(B, n, 1, (int64_t)L.bonds.size(), (int64_t)L.angles.size(), (int64_t)L.dihs.size(),
+                   (int64_t)L.inc_list.size(), (int64_t)L.ex_partner.size(), (int64_t)L.far_list.size(),
+                   2 * ((int64_t)L.cell_cap + 1));
+  if (rc != PRISMQ_OK) {
+    delete B;
+    return rc;
+  }
+  int slot = -1;
+  rc = batch_admit(B, L, *params, &slot);
+  if (rc != PRISMQ_OK) {
+    delete B;
+    return rc;
+  }
+  auto* s = new prismq_system();
+  s->b = B;
+  s->slot = slot;
+  *out = s;
+  return PRISMQ_OK;
+}
+
+void prismq_system_destroy(prismq_system* sys) {
+  if (!sys) return;
+  delete sys->b;
+  delete sys;
+}
+
+int32_t prismq_system_n_atoms(const prismq_system* sys) {
+  return sys ? (int32_t)sys->b->slots[sys->slot].n_atoms : 0;
+}
+
+static prismq_status set_param_field(prismq_system* sys, int which, float v) {
+  if (!sys) return fail(PRISMQ_E_INVALID, "system is NULL");
+  prismq_params p = sys->b->slots[sys->slot].params;
+  if (which == 0) p.dt = v;
+  if (which == 1) p.temperature = v;
+  if (which == 2) p.gamma = v;
+  prismq_status rc = check_params(&p);
+  if (rc != PRISMQ_OK) return rc;
+  prismq_batch* B = sys->b;
+  rc = B->sync_sys_from_device();
+  if (rc != PRISMQ_OK) return rc;
+  SysDev S = B->h_sys[sys->slot];
+  fill_params(&S, p);
+  PQ_CK(cudaMemcpyAsync(B->A.sys + sys->slot, &S, sizeof(S), cudaMemcpyHostToDevice, B->st));
+  PQ_CK(cudaStreamSynchronize(B->st));
+  B->slots[sys->slot].params = p;
+  return PRISMQ_OK;
+}
+
+prismq_status prismq_set_dt(prismq_system* sys, float dt) { return set_param_field(sys, 0, dt); }
+prismq_status prismq_set_temperature(prismq_system* sys, float t) { return set_param_field(sys, 1, t); }
+prismq_status prismq_set_gamma(prismq_system* sys, float g) { return set_param_field(sys, 2, g); }
+
+prismq_status prismq_set_positions(prismq_system* sys, const float* xyz) {
+  if (!sys || !xyz) return fail(PRISMQ_E_INVALID, "NULL argument");
+  return prismq_batch_set_state(sys->b, sys->slot, xyz, nullptr);
+}
+prismq_status prismq_set_velocities(prismq_system* sys, const float* vxyz) {
+  if (!sys || !vxyz) return fail(PRISMQ_E_INVALID, "NULL argument");
+  return prismq_batch_set_state(sys->b, sys->slot, nullptr, vxyz);
+}
+prismq_status prismq_get_positions(prismq_system* sys, float* xyz) {
+  if (!sys || !xyz) return fail(PRISMQ_E_INVALID, "NULL argument");
+  return prismq_batch_get_state(sys->b, sys->slot, xyz, nullptr);
+}
+prismq_status prismq_get_velocities(prismq_system* sys, float* vxyz) {
+  if (!sys || !vxyz) return fail(PRISMQ_E_INVALID, "NULL argument");
+  return prismq_batch_get_state(sys->b, sys->slot, nullptr, vxyz);
+}
+prismq_status prismq_get_step(prismq_system* sys, int64_t* step) {
+  if (!sys) return fail(PRISMQ_E_INVALID, "system is NULL");
+  return prismq_batch_get_step(sys->b, sys->slot, step);
+}
+prismq_status prismq_set_step(prismq_system* sys, int64_t step) {
+  if (!sys || step < 0) return fail(PRISMQ_E_INVALID, "invalid argument");
+  prismq_batch* B = sys->b;
+  const long long v = step;
+  PQ_CK(cudaMemcpyAsync(&B->A.sys[sys->slot].step, &v, sizeof(v), cudaMemcpyHostToDevice, B->st));
+  PQ_CK(cudaStreamSynchronize(B->st));
+  return PRISMQ_OK;
+}
+
+prismq_status prismq_step(prismq_system* sys, int64_t n_steps) {
+  if (!sys) return fail(PRISMQ_E_INVALID, "system is NULL");
+  if (n_steps < 0) return fail(PRISMQ_E_INVALID, "n_steps must be >= 0");
+  return sys->b->step(n_steps);
+}
+
+prismq_status prismq_compute_forces(prismq_system* sys, double* pe_total, float* f_aos, int64_t* f_fixed) {
+  if (!sys) return fail(PRISMQ_E_INVALID, "system is NULL");
+  prismq_batch* B = sys->b;
+  double e[6];
+  prismq_status rc = eval_energy(B, sys->slot, e);
+  if (rc != PRISMQ_OK) return rc;
+  if (pe_total) *pe_total = e[0] + e[1] + e[2] + e[3] + e[4];
+  if (f_aos || f_fixed) {
+    const SlotRec& R = B->slots[sys->slot];
+    const int64_t n = R.n_atoms;
+    std::vector<long long> h(3 * n);
+    for (int c = 0; c < 3; ++c)
+      PQ_CK(cudaMemcpyAsync(h.data() + c * n, B->A.f + c * B->A.atom_cap + R.atom_b, sizeof(long long) * n,
+                            cudaMemcpyDeviceToHost, B->st));
+    PQ_CK(cudaStreamSynchronize(B->st));
+    for (int64_t a = 0; a < n; ++a)
+      for (int c = 0; c < 3; ++c) {
+        const long long v = h[c * n + a];
+        if (f_fixed) f_fixed[3 * a + c] = v;
+        if (f_aos) f_aos[3 * a + c] = fixed2f(v);
+      }
+  }
+  return PRISMQ_OK;
+}
+
+prismq_status prismq_energy_components(prismq_system* sys, double out[6]) {
+  if (!sys || !out) return fail(PRISMQ_E_INVALID, "NULL argument");
+  return prismq_batch_energy(sys->b, sys->slot, out);
+}
+
+prismq_status prismq_build_neighbors(prismq_system* sys, prismq_nlist_mode mode, int32_t* pairs_out, size_t cap,
+                                     size_t* n_out) {
+  if (!sys || !n_out) return fail(PRISMQ_E_INVALID, "NULL argument");
+  if (mode != PRISMQ_NLIST_COMPLETE && mode != PRISMQ_NLIST_REF27) return fail(PRISMQ_E_INVALID, "unknown mode");
+  prismq_batch* B = sys->b;
+  const SlotRec& R = B->slots[sys->slot];
+  if (mode == PRISMQ_NLIST_REF27 && !R.ref_ok)
+    return fail(PRISMQ_E_INVALID, "reference grid needs more than 32 cells per axis for this system");
+  launch_control_cells(B->A, B->sys_span, kCtlForce, (int)mode, B->st);
+  launch_nbr_build(B->A, B->atom_span, 0, B->st);
+  g_launches += 2;
+  PQ_CK(cudaGetLastError());
+  const int64_t n = R.n_atoms, ab = R.atom_b;
+  std::vector<int> cnt(n);
+  PQ_CK(cudaMemcpyAsync(cnt.data(), B->A.nnbr + ab, sizeof(int) * n, cudaMemcpyDeviceToHost, B->st));
+  const int64_t g0 = ab / 32, g1 = (ab + n + 31) / 32;
+  std::vector<int> rows((size_t)(g1 - g0) * kNbrCap * 32);
+  PQ_CK(cudaMemcpyAsync(rows.data(), B->A.nbr + g0 * kNbrCap * 32, sizeof(int) * rows.size(),
+                        cudaMemcpyDeviceToHost, B->st));
+  PQ_CK(cudaStreamSynchronize(B->st));
+  prismq_status st = B->check_status(sys->slot);
+  // restore the production list
+  launch_control_cells(B->A, B->sys_span, kCtlForce, 0, B->st);
+  launch_nbr_build(B->A, B->atom_span, 1, B->st);
+  launch_force(B->A, B->atom_span, false, B->st);
+  g_launches += 3;
+  PQ_CK(cudaGetLastError());
+  PQ_CK(cudaStreamSynchronize(B->st));
+  if (st != PRISMQ_OK) return st;
+  std::vector<std::pair<int, int>> pairs;
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t a = ab + i;
+    const int64_t base = ((a / 32) - g0) * kNbrCap * 32 + (a & 31);
+    for (int k = 0; k < cnt[i]; ++k) {
+      const int j = rows[base + (int64_t)k * 32] - (int)ab;
+      if (j > i) pairs.emplace_back((int)i, j);
+    }
+  }
+  std::sort(pairs.begin(), pairs.end());
+  *n_out = pairs.size();
+  if (pairs.size() > cap || (!pairs_out && !pairs.empty()))
+    return fail(PRISMQ_E_CAPACITY, "pairs_out holds fewer than the pairs found");
+  for (size_t q = 0; q < pairs.size(); ++q) {
+    pairs_out[2 * q] = pairs[q].first;
+    pairs_out[2 * q + 1] = pairs[q].second;
+  }
+  return PRISMQ_OK;
+}
+
+prismq_status prismq_debug_phases(prismq_system* sys, prismq_phase_set set, int64_t step) {
+  if (!sys) return fail(PRISMQ_E_INVALID, "system is NULL");
+  if (set != PRISMQ_PHASES_PRE && set != PRISMQ_PHASES_POST) return fail(PRISMQ_E_INVALID, "unknown phase set");
+  prismq_batch* B = sys->b;
+  prismq_status rc = B->prime_if_needed();
+  if (rc != PRISMQ_OK) return rc;
+  launch_debug_phases(B->A, B->unit_span, set == PRISMQ_PHASES_PRE ? kIntPre : kIntPost, step, B->st);
+  g_launches += 1;
+  PQ_CK(cudaGetLastError());
+  PQ_CK(cudaStreamSynchronize(B->st));
+  return B->check_status(sys->slot);
+}
+
+}  // extern "C"

@@ -1,0 +1,459 @@
+// Per-system step control, cell lists and neighbour rows (compiled with --fmad=false).
+//
+// Reference path (nhs_amber_fused.cu:11690-11790, nhs_neighbor_warp.cuh:10-121,
+// fused_engine.rs:16615-16700): a fixed 10 Å grid from the construction-time
+// bounding box, cell slots claimed by atomicAdd, a warp-per-atom 27-cell scan
+// with r^2 <= (1.2·cutoff)^2, exclusion scan, and a per-row bitonic sort,
+// rebuilt every step.
+//
+// GB300 form:
+//   k_control_cells  one CTA per system: COM removal + deferred pre-phase on
+//                    COM steps, rebuild decision (interval or half-skin
+//                    displacement), bounding box, counting sort of atoms into
+//                    cells and an ascending sort of each cell's contents, so
+//                    that rows come out in a deterministic order without a
+//                    per-row sort.
+//   k_nbr_build      one CTA per 32-atom group (one warp per atom): 27-cell
+//                    scan, exclusion window bitmask, ballot compaction into
+//                    shared-memory rows, then a cooperative coalesced write of
+//                    the rows in the interleaved layout the force kernel reads.
+// Complete mode uses cells at least as wide as the list radius (every pair
+// within r_list is found); REF27 mode reproduces the reference pair set.
+#include "pq_phases.cuh"
+
+namespace pq {
+
+// r^2 in the reference's uncontracted FP32 order: (dx*dx + dy*dy) + dz*dz,
+// the order scripts/physics_refs/neighbor_list.py:63-91 evaluates.
+__device__ __forceinline__ float r2_nofma(float dx, float dy, float dz) {
+  return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+}
+
+constexpr int kCtlThreads = 1024;
+constexpr int kCellSortCap = 512;  // per-cell sort scratch (and overflow bound)
+
+__device__ __forceinline__ int cell_coord(float x, float lo, float inv_edge, int n) {
+  int c = (int)((x - lo) * inv_edge);
+  return c < 0 ? 0 : (c > n - 1 ? n - 1 : c);
+}
+
+__global__ void __launch_bounds__(kCtlThreads) k_control_cells(Arena A, int mode, int nbr_override) {
+  extern __shared__ int sm[];  // per-warp sort scratch: 32 * kCellSortCap ints
+  __shared__ long long red_i[3][32];
+  __shared__ double red_d[32];
+  __shared__ float red_f[6][32];
+  __shared__ int sh_rb;
+  __shared__ float sh_vcom[3];
+  const int s = blockIdx.x;
+  SysDev* Sp = &A.sys[s];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (!Sp->active) return;
+  if (Sp->status != 0) return;
+  const int ab = Sp->atom_begin, na = Sp->n_atoms;
+
+  if (mode == kCtlStep) {
+    const long long st = Sp->step;
+    const bool com = Sp->com_interval > 0 && st > 0 && (st % Sp->com_interval) == 0;
+    if (com) {
+      // Σ m·v as exact int64 fixed point, Σ m exactly in double.
+      long long px = 0, py = 0, pz = 0;
+      double m = 0.0;
+      for (int i = tid; i < na; i += kCtlThreads) {
+        const float4 v = A.vel[ab + i];
+        px += f2fixed(v.w * v.x);
+        py += f2fixed(v.w * v.y);
+        pz += f2fixed(v.w * v.z);
+        m += (double)v.w;
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        px += __shfl_xor_sync(0xffffffffu, px, o);
+        py += __shfl_xor_sync(0xffffffffu, py, o);
+        pz += __shfl_xor_sync(0xffffffffu, pz, o);
+        m += __shfl_xor_sync(0xffffffffu, m, o);
+      }
+      if (lane == 0) {
+        red_i[0][warp] = px;
+        red_i[1][warp] = py;
+        red_i[2][warp] = pz;
+        red_d[warp] = m;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        long long X = 0, Y = 0, Z = 0;
+        double M = 0.0;
+        for (int w = 0; w < 32; ++w) {
+          X += red_i[0][w];
+          Y += red_i[1][w];
+          Z += red_i[2][w];
+          M += red_d[w];
+        }
+        float cx = 0.0f, cy = 0.0f, cz = 0.0f;
+        if (M > 0.0) {
+          cx = (float)((double)X * kFixedInvD / M);
+          cy = (float)((double)Y * kFixedInvD / M);
+          cz = (float)((double)Z * kFixedInvD / M);
+        }
+        sh_vcom[0] = cx;
+        sh_vcom[1] = cy;
+        sh_vcom[2] = cz;
+        Sp->vcom[0] = cx;
+        Sp->vcom[1] = cy;
+        Sp->vcom[2] = cz;
+      }
+      __syncthreads();
+      const SysDev S = *Sp;
+      for (int t = tid; t < S.n_units; t += kCtlThreads) {
+        const Unit U = A.units[S.unit_begin + t];
+        if (U.nh < 0) continue;
+        UnitState u;
+        int local[4];
+        load_unit(A, U, u, local, ab);
+        for (int k = 0; k < u.n; ++k) {
+          u.vx[k] = u.vx[k] - sh_vcom[0];
+          u.vy[k] = u.vy[k] - sh_vcom[1];
+          u.vz[k] = u.vz[k] - sh_vcom[2];
+        }
+        int err = phases_pre(u, U, S, local, (uint64_t)st);
+        if (!err && !unit_finite(u)) err = kStNonfinite;
+        if (err) {
+          atomicOr(&Sp->status, err);
+          continue;
+        }
+        check_displacement(A, U, u, Sp);
+        store_unit(A, U, u);
+      }
+      __syncthreads();
+    }
+  }
+
+  if (tid == 0) {
+    bool rb;
+    const int disp = atomicAdd(&Sp->displaced, 0);
+    if (mode == kCtlPrime) {
+      rb = Sp->need_prime != 0;
+      Sp->need_prime = 0;
+    } else if (mode == kCtlForce) {
+      rb = true;
+    } else {
+      rb = !Sp->built || disp || Sp->steps_since_rebuild >= Sp->rebuild_interval;
+      Sp->step = Sp->step + 1;
+    }
+    if (atomicAdd(&Sp->status, 0) != 0) rb = false;
+    Sp->steps_since_rebuild = rb ? 1 : Sp->steps_since_rebuild + 1;
+    Sp->displaced = 0;
+    Sp->rebuilding = rb ? 1 : 0;
+    if (nbr_override >= 0 && rb) Sp->nbr_mode = nbr_override;
+    sh_rb = rb ? 1 : 0;
+  }
+  __syncthreads();
+  if (!sh_rb) return;
+
+  // ---- grid ----
+  const int nbr_mode = Sp->nbr_mode;
+  float lo[3], inv_edge[3];
+  int dims[3];
+  if (nbr_mode == 1) {
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = Sp->ref_origin[d];
+      inv_edge[d] = 0.1f;
+      dims[d] = Sp->ref_dims[d];
+    }
+  } else {
+    float mn[3] = {3.0e38f, 3.0e38f, 3.0e38f}, mx[3] = {-3.0e38f, -3.0e38f, -3.0e38f};
+    for (int i = tid; i < na; i += kCtlThreads) {
+      const float4 p = A.pos[ab + i];
+      mn[0] = fminf(mn[0], p.x);
+      mn[1] = fminf(mn[1], p.y);
+      mn[2] = fminf(mn[2], p.z);
+      mx[0] = fmaxf(mx[0], p.x);
+      mx[1] = fmaxf(mx[1], p.y);
+      mx[2] = fmaxf(mx[2], p.z);
+    }
+    for (int o = 16; o > 0; o >>= 1)
+      for (int d = 0; d < 3; ++d) {
+        mn[d] = fminf(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], o));
+        mx[d] = fmaxf(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], o));
+      }
+    if (lane == 0)
+      for (int d = 0; d < 3; ++d) {
+        red_f[d][warp] = mn[d];
+        red_f[3 + d][warp] = mx[d];
+      }
+    __syncthreads();
+    if (tid == 0) {
+      float gl[3], gh[3];
+      for (int d = 0; d < 3; ++d) {
+        gl[d] = red_f[d][0];
+        gh[d] = red_f[3 + d][0];
+        for (int w = 1; w < 32; ++w) {
+          gl[d] = fminf(gl[d], red_f[d][w]);
+          gh[d] = fmaxf(gh[d], red_f[3 + d][w]);
+        }
+      }
+      // cells at least r_list·(1+1e-4) wide on every axis
+      const float edge_min = sqrtf(Sp->rlist2) * 1.0001f;
+      int nd[3];
+      float ext[3];
+      for (int d = 0; d < 3; ++d) {
+        ext[d] = fmaxf(gh[d] - gl[d], 1.0e-3f);
+        const float q = ext[d] / edge_min;
+        nd[d] = q >= 1.0f ? (int)q : 1;
+        if (nd[d] > 1024) nd[d] = 1024;
+      }
+      while ((long long)nd[0] * nd[1] * nd[2] > Sp->cell_cap) {
+        int big = 0;
+        if (nd[1] > nd[big]) big = 1;
+        if (nd[2] > nd[big]) big = 2;
+        nd[big] -= 1;
+      }
+      for (int d = 0; d < 3; ++d) {
+        Sp->g_lo[d] = gl[d];
+        Sp->g_dims[d] = nd[d];
+        Sp->g_inv_edge[d] = (float)nd[d] / ext[d];
+      }
+    }
+    __syncthreads();
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = Sp->g_lo[d];
+      inv_edge[d] = Sp->g_inv_edge[d];
+      dims[d] = Sp->g_dims[d];
+    }
+  }
+  const int ncell = dims[0] * dims[1] * dims[2];
+  int* start = A.cell_start + Sp->cell_begin;     // ncell + 1 entries
+  int* cursor = start + (Sp->cell_cap + 1);       // ncell entries
+
+  // ---- counting sort ----
+  for (int c = tid; c <= ncell; c += kCtlThreads) start[c] = 0;
+  __syncthreads();
+  for (int i = tid; i < na; i += kCtlThreads) {
+    const int a = ab + i;
+    const float4 p = A.pos[a];
+    int ix, iy, iz;
+    if (nbr_mode == 1) {
+      // reference rule: truncate (x - origin) * 0.1f toward zero, then clamp
+      ix = (int)((p.x - lo[0]) * 0.1f);
+      iy = (int)((p.y - lo[1]) * 0.1f);
+      iz = (int)((p.z - lo[2]) * 0.1f);
+      ix = max(0, min(ix, dims[0] - 1));
+      iy = max(0, min(iy, dims[1] - 1));
+      iz = max(0, min(iz, dims[2] - 1));
+    } else {
+      ix = cell_coord(p.x, lo[0], inv_edge[0], dims[0]);
+      iy = cell_coord(p.y, lo[1], inv_edge[1], dims[1]);
+      iz = cell_coord(p.z, lo[2], inv_edge[2], dims[2]);
+    }
+    const int c = ix + iy * dims[0] + iz * dims[0] * dims[1];
+    A.atom_cell[a] = c;
+    atomicAdd(&start[c + 1], 1);
+  }
+  __syncthreads();
+  // exclusive scan (single-thread prefix over warp partials)
+  {
+    __shared__ int wsum[32];
+    __shared__ int carry;
+    if (tid == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < ncell; base += kCtlThreads) {
+      const int c = base + tid;
+      int v = c < ncell ? start[c + 1] : 0;
+      if (v > kCellSortCap) atomicOr(&Sp->status, kStCellOverflow);
+      int x = v;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+      }
+      if (lane == 31) wsum[warp] = x;
+      __syncthreads();
+      if (warp == 0) {
+        int w = wsum[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(0xffffffffu, w, o);
+          if (lane >= o) w += y;
+        }
+        wsum[lane] = w;
+      }
+      __syncthreads();
+      const int incl = x + (warp > 0 ? wsum[warp - 1] : 0) + carry;
+      if (c < ncell) {
+        start[c + 1] = incl;
+        cursor[c] = incl - v;
+      }
+      __syncthreads();
+      if (tid == kCtlThreads - 1) carry = incl;
+      __syncthreads();
+    }
+  }
+  if (atomicAdd(&Sp->status, 0) != 0) return;
+  for (int i = tid; i < na; i += kCtlThreads) {
+    const int a = ab + i;
+    const int c = A.atom_cell[a];
+    const int slot = atomicAdd(&cursor[c], 1);
+    A.cell_atoms[ab + slot] = a;
+  }
+  __syncthreads();
+  // ---- ascending order inside each cell (warp per cell, bitonic in smem) ----
+  int* buf = sm + warp * kCellSortCap;
+  for (int c = warp; c < ncell; c += kCtlThreads / 32) {
+    const int b = start[c], e = start[c + 1], n = e - b;
+    if (n <= 1) continue;
+    int p2 = 1;
+    while (p2 < n) p2 <<= 1;
+    for (int k = lane; k < p2; k += 32) buf[k] = k < n ? A.cell_atoms[ab + b + k] : 0x7fffffff;
+    __syncwarp();
+    for (int w = 2; w <= p2; w <<= 1) {
+      for (int st = w >> 1; st > 0; st >>= 1) {
+        for (int k = lane; k < p2; k += 32) {
+          const int q = k ^ st;
+          if (q > k) {
+            const int x = buf[k], y = buf[q];
+            const bool up = (k & w) == 0;
+            if ((up && x > y) || (!up && x < y)) {
+              buf[k] = y;
+              buf[q] = x;
+            }
+          }
+        }
+        __syncwarp();
+      }
+    }
+    for (int k = lane; k < n; k += 32) A.cell_atoms[ab + b + k] = buf[k];
+    __syncwarp();
+  }
+  if (tid == 0) {
+    Sp->built = 1;
+  }
+}
+
+// One CTA per 32-atom group; warp w builds the row of atom 32*group + w.
+constexpr int kNbrThreads = 1024;
+
+__global__ void __launch_bounds__(kNbrThreads) k_nbr_build(Arena A, int64_t n_span, int exclude_exc) {
+  extern __shared__ int rows[];  // [32][kNbrCap]
+  __shared__ int cnt[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t g = blockIdx.x;
+  const int64_t a64 = g * 32 + warp;
+  int count = -1;
+  int* row = rows + warp * kNbrCap;
+  if (a64 < n_span) {
+    const int a = (int)a64;
+    const int s = A.atom_sys[a];
+    SysDev* Sp = s >= 0 ? &A.sys[s] : nullptr;
+    if (Sp && Sp->active && Sp->rebuilding && Sp->status == 0) {
+      const int ab = Sp->atom_begin;
+      const int mode = Sp->nbr_mode;
+      int dims[3];
+      float r2max;
+      if (mode == 1) {
+        dims[0] = Sp->ref_dims[0];
+        dims[1] = Sp->ref_dims[1];
+        dims[2] = Sp->ref_dims[2];
+      } else {
+        dims[0] = Sp->g_dims[0];
+        dims[1] = Sp->g_dims[1];
+        dims[2] = Sp->g_dims[2];
+      }
+      r2max = mode == 1 ? Sp->ref_r2 : Sp->rlist2;
+      const int* start = A.cell_start + Sp->cell_begin;
+      const float4 pi = A.pos[a];
+      const int cell = A.atom_cell[a];
+      const int cx = cell % dims[0], cy = (cell / dims[0]) % dims[1], cz = cell / (dims[0] * dims[1]);
+      const unsigned long long mask = exclude_exc ? A.mask_all[a] : A.mask_ref[a];
+      const int2 far = A.far[a];
+      count = 0;
+      bool overflow = false;
+      for (int dz = -1; dz <= 1; ++dz) {
+        const int z = cz + dz;
+        if (z < 0 || z >= dims[2]) continue;
+        for (int dy = -1; dy <= 1; ++dy) {
+          const int y = cy + dy;
+          if (y < 0 || y >= dims[1]) continue;
+          for (int dx = -1; dx <= 1; ++dx) {
+            const int x = cx + dx;
+            if (x < 0 || x >= dims[0]) continue;
+            const int c = x + y * dims[0] + z * dims[0] * dims[1];
+            const int b = start[c], e = start[c + 1];
+            for (int base = b; base < e; base += 32) {
+              const int k = base + lane;
+              int j = 0;
+              bool keep = false;
+              if (k < e) {
+                j = A.cell_atoms[ab + k];
+                if (j != a) {
+                  const float4 pj = A.pos[j];
+                  const float r2 = r2_nofma(pj.x - pi.x, pj.y - pi.y, pj.z - pi.z);
+                  keep = !(r2 > r2max);
+                  if (keep) {
+                    const int d = j - a;
+                    if (d >= -32 && d < 32) {
+                      if ((mask >> (d + 32)) & 1ull) keep = false;
+                    } else {
+                      for (int q = 0; q < far.y; ++q) {
+                        const int ent = A.far_list[far.x + q];
+                        if ((ent & 0x3fffffff) == j && (exclude_exc || !(ent & 0x40000000))) {
+                          keep = false;
+                          break;
+                        }
+                      }
+                    }
+                  }
+                }
+              }
+              const unsigned bal = __ballot_sync(0xffffffffu, keep);
+              const int add = __popc(bal);
+              if (count + add > kNbrCap) {
+                overflow = true;
+              } else {
+                if (keep) row[count + __popc(bal & ((1u << lane) - 1u))] = j;
+                count += add;
+              }
+            }
+          }
+        }
+      }
+      if (overflow) {
+        if (lane == 0) atomicOr(&Sp->status, kStNbrOverflow);
+        count = -1;
+      } else if (lane == 0) {
+        A.nnbr[a] = count;
+        A.xref[a] = pi;
+      }
+    }
+  }
+  if (lane == 0) cnt[warp] = count;
+  __syncthreads();
+  // coalesced write of the interleaved rows: element (k, atom w) -> ((g*cap + k)*32 + w)
+  int maxc = 0;
+  for (int w = 0; w < 32; ++w) maxc = max(maxc, cnt[w]);
+  int* out = A.nbr + (g * kNbrCap) * 32;
+  for (int idx = threadIdx.x; idx < maxc * 32; idx += kNbrThreads) {
+    const int k = idx >> 5, w = idx & 31;
+    if (k < cnt[w]) out[idx] = rows[w * kNbrCap + k];
+  }
+}
+
+void launch_control_cells(const Arena& A, int n_sys, int mode, int nbr_override, cudaStream_t st) {
+  if (n_sys <= 0) return;
+  const size_t smem = (size_t)(kCtlThreads / 32) * kCellSortCap * sizeof(int);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_control_cells, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr = true;
+  }
+  k_control_cells<<<n_sys, kCtlThreads, smem, st>>>(A, mode, nbr_override);
+}
+
+void launch_nbr_build(const Arena& A, int64_t n_atoms_span, int exclude_exceptions, cudaStream_t st) {
+  if (n_atoms_span <= 0) return;
+  const size_t smem = (size_t)32 * kNbrCap * sizeof(int);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_nbr_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr = true;
+  }
+  const int64_t groups = (n_atoms_span + 31) / 32;
+  k_nbr_build<<<(unsigned)groups, kNbrThreads, smem, st>>>(A, n_atoms_span, exclude_exceptions);
+}
+
+}  // namespace pq

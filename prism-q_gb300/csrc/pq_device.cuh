@@ -1,0 +1,147 @@
+// Device data layout of the batched MD arena and the launchers of each kernel.
+//
+// All resident systems share one global atom index space.  Per-atom streams
+// are SoA float4 (position+charge, velocity+mass), float2 LJ, int64 forces
+// (three planes); bonded terms, exceptions and constraint units refer to
+// global atom indices.  One SysDev record per system carries its parameters
+// and the device-resident control state that a captured CUDA graph reads.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace pq {
+
+constexpr int kNbrCap = 1024;     // neighbour row capacity per atom
+constexpr int kRefCellCap = 512;  // REF27 cell capacity (MAX_ATOMS_PER_CELL)
+constexpr int kRefMaxDim = 32;    // REF27 cells per axis (MAX_CELLS_PER_DIM)
+
+// status bits of SysDev::status
+constexpr int kStShake = 1;
+constexpr int kStRattle = 2;
+constexpr int kStCellOverflow = 4;
+constexpr int kStNbrOverflow = 8;
+constexpr int kStNonfinite = 16;
+
+struct BondT {
+  int i, j;
+  float r0, k;
+};
+struct AngleT {
+  int i, j, k;
+  float theta0, kf;
+};
+struct DihT {
+  int i, j, k, l;
+  int n;
+  float phase, kf;
+};
+
+// A constraint unit: one H cluster (central + up to 3 H) or one lone atom.
+struct Unit {
+  int a[4];  // a[0] central / lone atom, a[1..3] hydrogens or -1
+  int nh;    // hydrogens (0 for a lone atom), -1 for an inactive slot
+  int sys;
+  float r0[3];
+  float inv_mc, inv_mh;
+  int pad;
+};
+
+struct SysDev {
+  // layout
+  int atom_begin, n_atoms, unit_begin, n_units;
+  int cell_begin, cell_cap;
+  int active;
+  int nbr_mode;  // 0 complete (production), 1 REF27 (parity only)
+  // parameters
+  float dt, temperature, gamma, c1;
+  float rlist2, half_skin2;
+  float ref_r2;  // REF27 list radius^2 = f32(cutoff^2) * 1.44f (fused_engine.rs:16674)
+  float cut2;    // potential cutoff^2
+  int rebuild_interval, com_interval, max_iter;
+  uint32_t seed, stream;
+  // REF27 grid fixed at admission (fused_engine.rs:12285-12330)
+  float ref_origin[3];
+  int ref_dims[3];
+  // dynamic control state
+  long long step;
+  int steps_since_rebuild;
+  int displaced;
+  int rebuilding;
+  int status;
+  int built;       // a list has been built at least once
+  int need_prime;  // set by the host when forces must be recomputed before stepping
+  // grid of the last build (complete mode)
+  float g_lo[3];
+  float g_inv_edge[3];
+  int g_dims[3];
+  int pad1;
+  double vcom[3];
+};
+
+// Per-atom incidence into bonded term arrays (reference: atom_bond_list etc.,
+// fused_engine.rs:11704-11745).  Entries are term_index*4 + position.
+struct Incidence {
+  int b_beg, a_beg, d_beg;
+  int counts;  // nb | na << 8 | nd << 16
+};
+
+struct Arena {
+  int64_t atom_cap = 0, unit_cap = 0, bond_cap = 0, angle_cap = 0, dih_cap = 0, inc_cap = 0,
+          ex_cap = 0, far_cap = 0, cell_cap = 0;
+  int sys_cap = 0;
+  // per atom
+  float4* pos = nullptr;   // x y z q
+  float4* vel = nullptr;   // vx vy vz mass
+  float2* lj = nullptr;    // sigma/2, sqrt(eps)
+  float4* xref = nullptr;  // positions at the last list build
+  long long* f = nullptr;  // 3 planes of atom_cap
+  double* pe = nullptr;    // 5 planes (bond, angle, dihedral, exception, nonbonded) of atom_cap
+  int* atom_sys = nullptr;
+  unsigned long long* mask_all = nullptr;  // exclusion window bits, offsets -32..31
+  unsigned long long* mask_ref = nullptr;  // same without exception pairs
+  int2* far = nullptr;                     // {begin, count} into far_list
+  int* far_list = nullptr;                 // partner | (is_exception << 30)
+  Incidence* inc = nullptr;
+  int* inc_list = nullptr;
+  int2* ex_idx = nullptr;     // {begin, count}
+  int* ex_partner = nullptr;  // global partner index
+  float4* ex_par = nullptr;   // qq, sigma, epsilon, 0
+  // terms
+  BondT* bonds = nullptr;
+  AngleT* angles = nullptr;
+  DihT* dihs = nullptr;
+  // constraint units
+  Unit* units = nullptr;
+  // lists
+  int* nbr = nullptr;   // interleaved rows: ((a>>5)*kNbrCap + k)*32 + (a&31)
+  int* nnbr = nullptr;  // row lengths
+  int* cell_start = nullptr;  // per system: cell_cap+1 entries
+  int* cell_atoms = nullptr;  // per atom (sorted by cell)
+  int* atom_cell = nullptr;
+  // systems
+  SysDev* sys = nullptr;
+};
+
+// K2 modes
+constexpr int kCtlPrime = 0;  // force a rebuild, no COM, no step increment
+constexpr int kCtlStep = 1;   // deferred COM pre-phase, rebuild decision, step increment
+constexpr int kCtlForce = 2;  // force a rebuild inside a step sequence (after set_positions)
+
+// K1 modes
+constexpr int kIntPre = 1;
+constexpr int kIntPost = 2;
+constexpr int kIntBoth = 3;
+
+// launchers (nbr.cu, force.cu, integrate.cu)
+void launch_control_cells(const Arena& A, int n_sys, int mode, int nbr_mode_override,
+                          cudaStream_t st);
+void launch_nbr_build(const Arena& A, int64_t n_atoms_span, int exclude_exceptions,
+                      cudaStream_t st);
+void launch_force(const Arena& A, int64_t n_atoms_span, bool energy, cudaStream_t st);
+void launch_integrate(const Arena& A, int64_t n_units_span, int mode, cudaStream_t st);
+void launch_debug_phases(const Arena& A, int64_t n_units_span, int set, long long step,
+                         cudaStream_t st);
+void launch_energy_reduce(const Arena& A, int n_sys, double* out6, cudaStream_t st);
+
+}  // namespace pq

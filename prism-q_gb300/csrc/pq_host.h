@@ -1,0 +1,54 @@
+// Host-side structures shared by the topology builder and the engine.
+#pragma once
+
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/prismq_md.h"
+
+namespace pq {
+
+// Owned copy of a prismq_topology (the builder's output, or a caller's input
+// after validation).
+struct HostTopology {
+  int32_t n_atoms = 0;
+  std::vector<float> positions, masses, charges, lj_sigma, lj_epsilon;
+  std::vector<prismq_bond> bonds;
+  std::vector<prismq_angle> angles;
+  std::vector<prismq_dihedral> dihedrals;
+  std::vector<prismq_exception> exceptions;
+  std::vector<int32_t> exclusion_offsets, exclusions;
+  std::vector<prismq_hcluster> clusters;
+
+  void view(prismq_topology* t) const {
+    t->n_atoms = n_atoms;
+    t->positions = positions.data();
+    t->masses = masses.data();
+    t->charges = charges.data();
+    t->lj_sigma = lj_sigma.data();
+    t->lj_epsilon = lj_epsilon.data();
+    t->n_bonds = (int32_t)bonds.size();
+    t->bonds = bonds.data();
+    t->n_angles = (int32_t)angles.size();
+    t->angles = angles.data();
+    t->n_dihedrals = (int32_t)dihedrals.size();
+    t->dihedrals = dihedrals.data();
+    t->n_exceptions = (int32_t)exceptions.size();
+    t->exceptions = exceptions.data();
+    t->exclusion_offsets = exclusion_offsets.data();
+    t->exclusions = exclusions.data();
+    t->n_clusters = (int32_t)clusters.size();
+    t->clusters = clusters.data();
+  }
+};
+
+bool polyala_build(int n_chains, int n_res, uint64_t seed, double density, double box_edge,
+                   HostTopology* T, std::string* err);
+
+}  // namespace pq
+
+struct prismq_topology_buf {
+  pq::HostTopology topo;
+};
