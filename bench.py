@@ -1,0 +1,402 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 MD step (aggregate atom-steps/s, batched vs plain).
+
+Default workload: the batched ensemble — 256 independent seeded poly-alanine
+systems, chain lengths log-uniform in 50–800 residues (500–8,000 atoms), each
+with its own Philox stream, advanced together (one launch per phase, CUDA
+graph).  One "step" is one MD step of every resident system.
+
+Printed (rank 0, one JSON line): value = whole-job device throughput with the
+state resident in HBM (CUDA events on the library's stream around a graph of K
+steps); e2e = the same metric through the C ABI with host state uploaded from
+pinned memory and read back every step; roofline of the force kernel (CUDA
+events around every force launch inside the timed graph); the plain
+one-system-at-a-time loop on a stratified sample of the same systems; the CPU
+baseline (the oracle's restatement of the reference step, all host threads).
+
+--impl reference times the reference's CPU step (oracle restatement; the
+reference ships no CPU implementation and its Rust host cannot be built) on a
+stratified sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import importlib
+import json
+import math
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "aggregate atom-steps/s, batched vs plain, 1 GB300; p50/p99 job latency"
+FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12  # SMs x FP32 lanes x FMA x max SM clock
+
+
+def args_parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="batch256", choices=["batch256", "plain2500", "large100k"])
+    ap.add_argument("--systems", type=int, default=256)
+    ap.add_argument("--seed", type=int, default=20261203)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ workload
+def workload_sizes(kind: str, nsys: int, seed: int) -> list[tuple[int, int, float]]:
+    """(n_chains, n_residues, box_edge) per system."""
+    if kind == "plain2500":
+        return [(1, 250, 0.0)]
+    if kind == "large100k":
+        return [(40, 250, 110.0)]
+    rng = np.random.default_rng(seed)
+    res = np.exp(rng.uniform(math.log(50), math.log(800), size=nsys))
+    return [(1, int(round(r)), 0.0) for r in res]
+
+
+def build_topologies(pq, specs, indices, seed):
+    def one(i):
+        c, r, box = specs[i]
+        return pq.Topology.polyala(c, r, seed=seed + 7919 * i, box_edge=box)
+
+    with ThreadPoolExecutor(max_workers=min(32, os.cpu_count() or 4)) as ex:
+        return list(ex.map(one, indices))
+
+
+def pair_stats(topo) -> dict:
+    """Unique ordinary pairs within 10 Å (P10) and bonded term counts."""
+    from scipy.spatial import cKDTree
+
+    p = topo.positions.astype(np.float64)
+    t = cKDTree(p)
+    within = (int(t.count_neighbors(t, 10.0)) - len(p)) // 2
+    excl = len(topo.exclusions) // 2
+    return {"atoms": topo.n_atoms, "p10": max(within - excl, 0), "bonds": len(topo.bonds),
+            "angles": len(topo.angles), "dihedrals": len(topo.dihedrals), "exceptions": len(topo.exceptions)}
+
+
+def flops_per_step(st: dict) -> float:
+    # algorithmic FLOPs per step of one system: 36 per ordinary pair within the
+    # cutoff and per exception, 25/60/90 per bond/angle/torsion term, 60 per atom
+    return (36.0 * (st["p10"] + st["exceptions"]) + 25.0 * st["bonds"] + 60.0 * st["angles"] +
+            90.0 * st["dihedrals"] + 60.0 * st["atoms"])
+
+
+def bytes_per_step(st: dict, list_len: float = 0.0) -> float:
+    # x (16) + v r/w (32) + int64 forces w/r (48) + per-atom params (16) + x_start (16) per atom
+    return st["atoms"] * (128.0 + 4.0 * list_len / 20.0)
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    def __init__(self):
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        idx = os.environ.get("LOCAL_RANK", "0")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", idx, f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict | None:
+        if not self.proc:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[4:8]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ distributed
+def dist_setup(n_gpus: int):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    import torch
+
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(v: float, world: int) -> float:
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(v: float, world: int) -> float:
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------ CPU legs
+def stratified(n: int, k: int) -> list[int]:
+    if n <= k:
+        return list(range(n))
+    return sorted({int(round(i * (n - 1) / (k - 1))) for i in range(k)})
+
+
+def cpu_reference_rate(pq, topos, steps_cap: int, seconds: float, threads: int) -> tuple[float, str]:
+    """Oracle restatement of the reference step loop; returns atom-steps/s."""
+    from oracle import oracle as orc
+
+    orc.build()
+    p = pq.Params()
+    atoms_steps, wall = 0, 0.0
+    desc = []
+    budget = seconds / max(len(topos), 1)
+    for t in topos:
+        o = orc.OracleSystem(t.struct(), seed=p.seed, stream=p.stream)
+        eng_v = np.zeros((t.n_atoms, 3), np.float32)
+        o.set_state(t.positions, eng_v)
+        t0 = time.perf_counter()
+        o.run(1, threads)
+        one = max(time.perf_counter() - t0, 1e-4)
+        n = int(max(1, min(steps_cap, budget / one)))
+        t0 = time.perf_counter()
+        rc = o.run(n, threads)
+        dt = time.perf_counter() - t0
+        if rc:
+            raise RuntimeError(f"oracle step failed ({rc})")
+        atoms_steps += t.n_atoms * n
+        wall += dt
+        desc.append(f"{t.n_atoms}x{n}")
+        o.close()
+    return atoms_steps / wall, ", ".join(desc)
+
+
+# ------------------------------------------------------------------ main legs
+def run_reference(args, pq, rank, world):
+    if rank != 0:
+        return
+    specs = workload_sizes(args.workload, args.systems, args.seed)
+    idx = stratified(len(specs), 4 if args.workload == "batch256" else 1)
+    topos = build_topologies(pq, specs, idx, args.seed)
+    threads = os.cpu_count() or 1
+    cpu_reference_rate(pq, topos[:1], 2, 1.0, threads)  # warm-up: page in, spin up the thread pool
+    value, desc = cpu_reference_rate(pq, topos, max(args.steps, 1), 30.0, threads)
+    line = {"metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "impl": "reference", "dtype": "f32",
+            "data": "synthetic (seeded poly-alanine systems)",
+            "config": {"workload": args.workload, "systems_sampled": len(topos), "sample": desc},
+            "cpu_baseline": {"value": value, "unit": "atom-steps/s", "cores": threads, "kind": "port",
+                             "sample": f"oracle restatement of the reference step loop on {desc} (atoms x steps)"},
+            "e2e": {"value": value, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "vs_baseline": None}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, pq, rank, world):
+    import torch
+
+    specs = workload_sizes(args.workload, args.systems, args.seed)
+    mine = [i for i in range(len(specs)) if i % world == rank]
+    topos = build_topologies(pq, specs, mine, args.seed)
+    atoms = sum(t.n_atoms for t in topos)
+    batch = pq.Batch(max_atoms=atoms + 64 * len(topos), max_systems=len(topos))
+    slots = []
+    for i, t in zip(mine, topos):
+        slots.append(batch.add_system(t, pq.Params(stream=i)))
+    batch.step(max(args.warmup, 3))
+    # pair statistics at the warmed-up positions
+    stats = []
+    for s, t in zip(slots, topos):
+        x, _ = batch.get_state(s)
+        tt = pq.Topology(x, t.masses, t.charges, t.lj_sigma, t.lj_epsilon, t.bonds, t.angles, t.dihedrals,
+                         t.exceptions, t.exclusion_offsets, t.exclusions, t.clusters)
+        stats.append(pair_stats(tt))
+    flops_launch = sum(flops_per_step(s) for s in stats)
+    p10_mean = sum(s["p10"] for s in stats) / max(atoms, 1)
+    # ---------------- timed device region
+    clocks = ClockSampler()
+    launches0 = pq.kernel_launches()
+    barrier(world)
+    clocks.start()
+    total_ms = ctypes.c_float()
+    force_ms = (ctypes.c_float * args.steps)()
+    rc = pq.load().prismq_batch_run_timed(batch.h, args.steps, ctypes.addressof(total_ms),
+                                          ctypes.addressof(force_ms))
+    if rc:
+        raise pq.PrismQError(rc, pq.load().prismq_last_error().decode())
+    clk = clocks.stop()
+    barrier(world)
+    launches = pq.kernel_launches() - launches0
+    t_max = max_over_ranks(total_ms.value / 1e3, world)
+    total_atoms = sum_over_ranks(float(atoms), world)
+    value = total_atoms * args.steps / t_max
+    f_avg_ms = statistics.mean(force_ms[i] for i in range(args.steps))
+    achieved = flops_launch / (f_avg_ms / 1e3) / 1e12
+    # ---------------- e2e through the C ABI with pinned host buffers
+    span = int(pq.load().prismq_batch_atom_span(batch.h))
+    hx = torch.empty(3 * span, dtype=torch.float32, pin_memory=True).numpy()
+    hv = torch.empty(3 * span, dtype=torch.float32, pin_memory=True).numpy()
+    L = pq.load()
+    L.prismq_batch_get_state_all(batch.h, hx.ctypes.data, hv.ctypes.data)
+    for _ in range(2):
+        L.prismq_batch_set_state_all(batch.h, hx.ctypes.data, hv.ctypes.data)
+        batch.step(1)
+        L.prismq_batch_get_state_all(batch.h, hx.ctypes.data, hv.ctypes.data)
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        rc = L.prismq_batch_set_state_all(batch.h, hx.ctypes.data, hv.ctypes.data)
+        rc |= L.prismq_batch_step(batch.h, 1)
+        rc |= L.prismq_batch_get_state_all(batch.h, hx.ctypes.data, hv.ctypes.data)
+        if rc:
+            raise pq.PrismQError(rc, L.prismq_last_error().decode())
+    e2e_t = max_over_ranks(time.perf_counter() - t0, world)
+    e2e_value = total_atoms * args.e2e_steps / e2e_t
+    # ---------------- plain loop (one system at a time) on a stratified sample
+    plain_value = None
+    if world == 1 and len(topos) > 1 and not args.no_plain:
+        pick = stratified(len(topos), 8)
+        a_sum, t_sum = 0, 0.0
+        for k in pick:
+            eng = pq.NhsAmberFusedEngine(topos[k], pq.Params(stream=mine[k]))
+            eng.step(3)
+            n = 200
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            eng.step(n)
+            dt = time.perf_counter() - t0
+            a_sum += topos[k].n_atoms * n
+            t_sum += dt
+            eng.close()
+        plain_value = a_sum / t_sum
+    # ---------------- CPU baseline (rank 0, N = 1)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        pick = stratified(len(topos), 3)
+        threads = os.cpu_count() or 1
+        rate, desc = cpu_reference_rate(pq, [topos[k] for k in pick], 400, 20.0, threads)
+        cpu = {"value": rate, "unit": "atom-steps/s", "cores": threads, "kind": "port",
+               "sample": f"oracle restatement of the reference step loop (per-step REF27 rebuild, two FP32 force "
+                         f"evaluations per step), systems atoms x steps: {desc}"}
+    traffic = None
+    tf = ROOT / "profiles" / "force_traffic.txt"
+    if tf.exists():
+        for ln in tf.read_text().splitlines():
+            if ln.startswith("dram_bytes_per_atom_step"):
+                traffic = float(ln.split()[1]) * atoms
+    roof = {"bound": "fp32", "achieved": achieved, "peak": FP32_PEAK_TFLOPS, "unit": "TFLOP/s",
+            "frac": achieved / FP32_PEAK_TFLOPS, "traffic": traffic,
+            "peak_source": "nominal FP32 SIMT peak (152 SMs x 128 lanes x 2 x 2.07 GHz); MEASURED_PEAKS has no FP32 entry",
+            "kernel": "k_force", "kernel_avg_ms": f_avg_ms, "flops_per_launch": flops_launch}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+        hbm_peak = float(peaks["hbm_gbs"])
+    except (OSError, ValueError, KeyError):
+        hbm_peak = 6800.0
+    step_bytes = sum(bytes_per_step(s) for s in stats)
+    hbm = {"achieved_gbs": step_bytes * args.steps / t_max / 1e9, "peak_gbs": hbm_peak,
+           "frac": step_bytes * args.steps / t_max / 1e9 / hbm_peak}
+    line = {
+        "metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded poly-alanine systems; no dataset)",
+        "config": {"workload": args.workload, "systems": len(specs), "atoms_total": int(total_atoms),
+                   "atoms_rank0": atoms, "p10_per_atom": p10_mean,
+                   "parallelism": f"independent systems sharded over {world} GPU(s)",
+                   "l2": "inputs larger than L2 (neighbour rows ~4 KiB/atom, re-read every step)"},
+        "e2e": {"value": e2e_value, "unit": "atom-steps/s", "h2d_bytes_per_step": 24 * span,
+                "d2h_bytes_per_step": 24 * span, "steps": args.e2e_steps},
+        "plain": None if plain_value is None else {"value": plain_value, "unit": "atom-steps/s",
+                                                   "batched_over_plain": value / plain_value,
+                                                   "sample": "8 stratified systems run alone, 200 steps each"},
+        "roofline": roof, "hbm": hbm, "gpu_launches": int(launches), "clocks": clk, "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    batch.close()
+
+
+def main():
+    args = args_parse()
+    import __graft_entry__
+
+    __graft_entry__.build()
+    pq = importlib.import_module("prism-q_gb300")
+    rank, world, _ = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, pq, rank, world)
+    else:
+        run_ours(args, pq, rank, world)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -235,6 +235,19 @@ prismq_status prismq_batch_get_step(prismq_batch* b, int32_t slot, int64_t* step
 prismq_status prismq_batch_status(prismq_batch* b, int32_t slot);
 prismq_status prismq_batch_energy(prismq_batch* b, int32_t slot, double out[6]);
 int64_t prismq_batch_resident_atoms(const prismq_batch* b);
+/* Whole-arena state transfer: float[3*span] in arena atom order (span =
+ * prismq_batch_atom_span; system `slot` starts at prismq_batch_atom_offset).
+ * Entries of free arena ranges are ignored on upload.  Uploaded positions that
+ * differ bitwise from the resident ones refresh that system's list and forces
+ * before its next step. */
+int64_t prismq_batch_atom_span(const prismq_batch* b);
+int64_t prismq_batch_atom_offset(const prismq_batch* b, int32_t slot);
+prismq_status prismq_batch_set_state_all(prismq_batch* b, const float* xyz, const float* vxyz);
+prismq_status prismq_batch_get_state_all(prismq_batch* b, float* xyz, float* vxyz);
+/* Advance every resident system by n_steps+1 steps, of which n_steps are
+ * captured in one CUDA graph and timed on the device: total_ms covers those
+ * n_steps, force_ms[i] (optional, n_steps entries) the force launch of step i. */
+prismq_status prismq_batch_run_timed(prismq_batch* b, int64_t n_steps, float* total_ms, float* force_ms);
 int32_t prismq_batch_resident_systems(const prismq_batch* b);
 
 #ifdef __cplusplus

@@ -144,6 +144,11 @@ def load() -> ctypes.CDLL:
         "prismq_batch_energy": (I, [P, ctypes.c_int32, P]),
         "prismq_batch_resident_atoms": (i64, [P]),
         "prismq_batch_resident_systems": (ctypes.c_int32, [P]),
+        "prismq_batch_atom_span": (i64, [P]),
+        "prismq_batch_atom_offset": (i64, [P, ctypes.c_int32]),
+        "prismq_batch_set_state_all": (I, [P, P, P]),
+        "prismq_batch_get_state_all": (I, [P, P, P]),
+        "prismq_batch_run_timed": (I, [P, i64, P, P]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(L, name)

@@ -319,7 +319,7 @@ prismq_status lower_topology(const prismq_topology* T, Lowered* L) {
     L->ref_dims[d] = (int)std::min<long long>(v, kRefMaxDim);
     ref_cells *= L->ref_dims[d];
   }
-  L->cell_cap = (int)std::max<long long>({64LL, (long long)n / 32, L->ref_ok ? ref_cells : 0LL});
+  L->cell_cap = (int)std::max<long long>({512LL, (long long)n / 4, L->ref_ok ? ref_cells : 0LL});
   return PRISMQ_OK;
 }
 
@@ -397,6 +397,43 @@ __global__ void k_xyz_to_aos(float* dst, const float4* src, int n) {
   dst[3 * i + 1] = v.y;
   dst[3 * i + 2] = v.z;
 }
+// Whole-arena state upload: positions whose bits change mark their system for
+// a force/list refresh before the next step.
+__global__ void k_set_state_all(float4* pos, float4* vel, const float* xs, const float* vs, const int* atom_sys,
+                                SysDev* sys, int64_t n) {
+  const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= n) return;
+  const int s = atom_sys[a];
+  if (s < 0) return;
+  if (xs) {
+    const float4 o = pos[a];
+    const float x = xs[3 * a], y = xs[3 * a + 1], z = xs[3 * a + 2];
+    if (__float_as_uint(x) != __float_as_uint(o.x) || __float_as_uint(y) != __float_as_uint(o.y) ||
+        __float_as_uint(z) != __float_as_uint(o.z)) {
+      pos[a] = make_float4(x, y, z, o.w);
+      atomicOr(&sys[s].need_prime, 1);
+    }
+  }
+  if (vs) {
+    const float4 o = vel[a];
+    vel[a] = make_float4(vs[3 * a], vs[3 * a + 1], vs[3 * a + 2], o.w);
+  }
+}
+__global__ void k_get_state_all(const float4* pos, const float4* vel, float* xs, float* vs, int64_t n) {
+  const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= n) return;
+  const float4 p = pos[a], v = vel[a];
+  if (xs) {
+    xs[3 * a] = p.x;
+    xs[3 * a + 1] = p.y;
+    xs[3 * a + 2] = p.z;
+  }
+  if (vs) {
+    vs[3 * a] = v.x;
+    vs[3 * a + 1] = v.y;
+    vs[3 * a + 2] = v.z;
+  }
+}
 __global__ void k_fill_int(int* p, int v, int64_t n) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) p[i] = v;
@@ -429,6 +466,7 @@ struct prismq_batch {
   int sys_span = 0;
   double* d_energy = nullptr;
   float* d_stage = nullptr;
+  float* d_stage2 = nullptr;
   std::vector<SysDev> h_sys;
 
   ~prismq_batch() {
@@ -436,7 +474,7 @@ struct prismq_batch {
     void* ptrs[] = {A.pos, A.vel, A.lj, A.xref, A.f, A.pe, A.atom_sys, A.mask_all, A.mask_ref, A.far,
                     A.far_list, A.inc, A.inc_list, A.ex_idx, A.ex_partner, A.ex_par, A.bonds, A.angles,
                     A.dihs, A.units, A.nbr, A.nnbr, A.cell_start, A.cell_atoms, A.atom_cell, A.sys,
-                    d_energy, d_stage};
+                    d_energy, d_stage, d_stage2};
     for (void* p : ptrs)
       if (p) cudaFree(p);
     if (st) cudaStreamDestroy(st);
@@ -489,9 +527,14 @@ struct prismq_batch {
     for (auto& s : slots)
       if (s.active && s.need_prime) any = true;
     if (!any) return PRISMQ_OK;
+    return prime_flagged();
+  }
+
+  // Refresh lists and forces of the systems whose device need_prime flag is set.
+  prismq_status prime_flagged() {
     launch_control_cells(A, sys_span, kCtlPrime, -1, st);
     launch_nbr_build(A, atom_span, 1, st);
-    launch_force(A, atom_span, false, st);
+    launch_force(A, atom_span, false, st, true);
     g_launches += 3;
     PQ_CK(cudaGetLastError());
     for (auto& s : slots) s.need_prime = false;
@@ -517,6 +560,49 @@ struct prismq_batch {
     if (stt & kStCellOverflow) return fail(PRISMQ_E_CELL_OVERFLOW, "cell occupancy above 512" + where);
     if (stt & kStNbrOverflow) return fail(PRISMQ_E_NEIGHBOR_OVERFLOW, "neighbour row above 1024" + where);
     return fail(PRISMQ_E_NONFINITE, "non-finite state" + where);
+  }
+
+  // n steady steps captured in one graph with an event pair around every force
+  // launch; head and tail phases run outside the timed graph.
+  prismq_status run_timed(int64_t n, float* total_ms, float* force_ms) {
+    if (n <= 0 || sys_span == 0) return fail(PRISMQ_E_INVALID, "nothing to time");
+    prismq_status rc = prime_if_needed();
+    if (rc != PRISMQ_OK) return rc;
+    std::vector<cudaEvent_t> ev(2 * n + 2);
+    for (auto& e : ev) PQ_CK(cudaEventCreate(&e));
+    launch_integrate(A, unit_span, kIntPre, st);
+    g_launches += 1;
+    cudaGraph_t g;
+    cudaGraphExec_t ge = nullptr;
+    PQ_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    cudaEventRecordWithFlags(ev[0], st, cudaEventRecordExternal);
+    for (int64_t i = 0; i < n; ++i) {
+      launch_control_cells(A, sys_span, kCtlStep, -1, st);
+      launch_nbr_build(A, atom_span, 1, st);
+      cudaEventRecordWithFlags(ev[2 + 2 * i], st, cudaEventRecordExternal);
+      launch_force(A, atom_span, false, st);
+      cudaEventRecordWithFlags(ev[3 + 2 * i], st, cudaEventRecordExternal);
+      launch_integrate(A, unit_span, kIntBoth, st);
+    }
+    cudaEventRecordWithFlags(ev[1], st, cudaEventRecordExternal);
+    PQ_CK(cudaStreamEndCapture(st, &g));
+    cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    PQ_CK(e);
+    PQ_CK(cudaStreamSynchronize(st));
+    PQ_CK(cudaGraphLaunch(ge, st));
+    g_launches += 4 * n;
+    PQ_CK(cudaStreamSynchronize(st));
+    PQ_CK(cudaEventElapsedTime(total_ms, ev[0], ev[1]));
+    if (force_ms)
+      for (int64_t i = 0; i < n; ++i) PQ_CK(cudaEventElapsedTime(&force_ms[i], ev[2 + 2 * i], ev[3 + 2 * i]));
+    cudaGraphExecDestroy(ge);
+    for (auto& x : ev) cudaEventDestroy(x);
+    enqueue_step_body();
+    launch_integrate(A, unit_span, kIntPost, st);
+    g_launches += 4;
+    PQ_CK(cudaGetLastError());
+    return check_status();
   }
 
   prismq_status step(int64_t n) {
@@ -597,6 +683,7 @@ prismq_status batch_alloc(prismq_batch* B, int64_t atom_cap, int sys_cap, int64_
   PQ_ALLOC(A.sys, sys_cap);
   PQ_ALLOC(B->d_energy, 6 * (int64_t)sys_cap);
   PQ_ALLOC(B->d_stage, 3 * atom_cap);
+  PQ_ALLOC(B->d_stage2, 3 * atom_cap);
 #undef PQ_ALLOC
   PQ_CK(cudaMemsetAsync(A.sys, 0, sizeof(SysDev) * sys_cap, B->st));
   PQ_CK(cudaMemsetAsync(A.nnbr, 0, sizeof(int) * atom_cap, B->st));
@@ -906,7 +993,7 @@ prismq_status prismq_batch_create(int64_t max_atoms, int32_t max_systems, prismq
   auto* B = new prismq_batch();
   const int64_t na = (max_atoms + 31) / 32 * 32 + 32 * (int64_t)max_systems;
   prismq_status rc = batch_alloc(B, na, max_systems, 2 * na, 4 * na, 8 * na, 48 * na, 8 * na, 2 * na,
-                                 2 * (na / 8 + 130 * (int64_t)max_systems));
+                                 2 * (na / 4 + 514 * (int64_t)max_systems));
   if (rc != PRISMQ_OK) {
     delete B;
     return rc;
@@ -986,6 +1073,47 @@ prismq_status prismq_batch_energy(prismq_batch* b, int32_t slot, double out[6]) 
   if (rc != PRISMQ_OK) return rc;
   // five potential planes in order: bond, angle, dihedral, exception, nonbonded; then kinetic
   for (int i = 0; i < 6; ++i) out[i] = e[i];
+  return PRISMQ_OK;
+}
+
+prismq_status prismq_batch_run_timed(prismq_batch* b, int64_t n_steps, float* total_ms, float* force_ms) {
+  if (!b || !total_ms) return fail(PRISMQ_E_INVALID, "NULL argument");
+  return b->run_timed(n_steps, total_ms, force_ms);
+}
+
+int64_t prismq_batch_atom_span(const prismq_batch* b) { return b ? b->atom_span : 0; }
+
+int64_t prismq_batch_atom_offset(const prismq_batch* b, int32_t slot) {
+  if (!b || slot < 0 || slot >= (int)b->slots.size() || !b->slots[slot].active) return -1;
+  return b->slots[slot].atom_b;
+}
+
+prismq_status prismq_batch_set_state_all(prismq_batch* b, const float* xyz, const float* vxyz) {
+  if (!b) return fail(PRISMQ_E_INVALID, "batch is NULL");
+  const int64_t n = b->atom_span;
+  if (n == 0) return PRISMQ_OK;
+  if (xyz) PQ_CK(cudaMemcpyAsync(b->d_stage, xyz, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, b->st));
+  if (vxyz) PQ_CK(cudaMemcpyAsync(b->d_stage2, vxyz, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, b->st));
+  k_set_state_all<<<(unsigned)((n + 255) / 256), 256, 0, b->st>>>(b->A.pos, b->A.vel, xyz ? b->d_stage : nullptr,
+                                                                   vxyz ? b->d_stage2 : nullptr, b->A.atom_sys,
+                                                                   b->A.sys, n);
+  g_launches += 1;
+  PQ_CK(cudaGetLastError());
+  if (xyz) return b->prime_flagged();
+  return PRISMQ_OK;
+}
+
+prismq_status prismq_batch_get_state_all(prismq_batch* b, float* xyz, float* vxyz) {
+  if (!b) return fail(PRISMQ_E_INVALID, "batch is NULL");
+  const int64_t n = b->atom_span;
+  if (n == 0) return PRISMQ_OK;
+  k_get_state_all<<<(unsigned)((n + 255) / 256), 256, 0, b->st>>>(b->A.pos, b->A.vel, xyz ? b->d_stage : nullptr,
+                                                                   vxyz ? b->d_stage2 : nullptr, n);
+  g_launches += 1;
+  PQ_CK(cudaGetLastError());
+  if (xyz) PQ_CK(cudaMemcpyAsync(xyz, b->d_stage, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, b->st));
+  if (vxyz) PQ_CK(cudaMemcpyAsync(vxyz, b->d_stage2, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, b->st));
+  PQ_CK(cudaStreamSynchronize(b->st));
   return PRISMQ_OK;
 }
 
@@ -1151,9 +1279,9 @@ prismq_status prismq_build_neighbors(prismq_system* sys, prismq_nlist_mode mode,
   const int64_t n = R.n_atoms, ab = R.atom_b;
   std::vector<int> cnt(n);
   PQ_CK(cudaMemcpyAsync(cnt.data(), B->A.nnbr + ab, sizeof(int) * n, cudaMemcpyDeviceToHost, B->st));
-  const int64_t g0 = ab / 32, g1 = (ab + n + 31) / 32;
-  std::vector<int> rows((size_t)(g1 - g0) * kNbrCap * 32);
-  PQ_CK(cudaMemcpyAsync(rows.data(), B->A.nbr + g0 * kNbrCap * 32, sizeof(int) * rows.size(),
+  const int64_t g0 = ab / 8, g1 = (ab + n + 7) / 8;
+  std::vector<int> rows((size_t)(g1 - g0) * kNbrCap * 8);
+  PQ_CK(cudaMemcpyAsync(rows.data(), B->A.nbr + g0 * kNbrCap * 8, sizeof(int) * rows.size(),
                         cudaMemcpyDeviceToHost, B->st));
   PQ_CK(cudaStreamSynchronize(B->st));
   prismq_status st = B->check_status(sys->slot);
@@ -1168,9 +1296,8 @@ prismq_status prismq_build_neighbors(prismq_system* sys, prismq_nlist_mode mode,
   std::vector<std::pair<int, int>> pairs;
   for (int64_t i = 0; i < n; ++i) {
     const int64_t a = ab + i;
-    const int64_t base = ((a / 32) - g0) * kNbrCap * 32 + (a & 31);
     for (int k = 0; k < cnt[i]; ++k) {
-      const int j = rows[base + (int64_t)k * 32] - (int)ab;
+      const int j = rows[nbr_index(a, k) - g0 * kNbrCap * 8] - (int)ab;
       if (j > i) pairs.emplace_back((int)i, j);
     }
   }

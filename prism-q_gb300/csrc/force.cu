@@ -142,33 +142,52 @@ __device__ __forceinline__ float pair_scalar(float r2, float sig, float eps, flo
   return flj + fc;
 }
 
+// Sum an int64 over the 4 lanes of one atom (fixed butterfly: exact, order-free).
+__device__ __forceinline__ long long lane_sum(long long v) {
+  v += __shfl_xor_sync(0xffffffffu, v, 1);
+  v += __shfl_xor_sync(0xffffffffu, v, 2);
+  return v;
+}
+__device__ __forceinline__ double lane_sum(double v) {
+  v += __shfl_xor_sync(0xffffffffu, v, 1);
+  v += __shfl_xor_sync(0xffffffffu, v, 2);
+  return v;
+}
+
+// Four lanes per atom: lane q takes bonded terms, exceptions and row entries
+// with index ≡ q (mod 4).  Each lane keeps FP32 partial sums over at most 32 of
+// its entries and accumulates them in int64; the lanes' int64 totals are then
+// summed exactly.  The decomposition depends only on the atom's own lists, so
+// an atom's force is identical whatever batch it is computed in.
 template <bool kEnergy>
-__global__ void __launch_bounds__(128) k_force(Arena A, int64_t n_span) {
-  const int64_t a64 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (a64 >= n_span) return;
-  const int a = (int)a64;
-  const int s = A.atom_sys[a];
-  if (s < 0) return;
-  const SysDev& S = A.sys[s];
-  if (!S.active) return;
-  const float cut2 = S.cut2;
+__global__ void __launch_bounds__(128) k_force(Arena A, int64_t n_span, int only_rebuilt) {
+  const int64_t a64 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 2;
+  const int q = threadIdx.x & 3;
+  bool live = a64 < n_span;
+  const int a = live ? (int)a64 : 0;
+  const int s = live ? A.atom_sys[a] : -1;
+  live = live && s >= 0;
+  const SysDev* Sp = live ? &A.sys[s] : nullptr;
+  live = live && Sp->active && (!only_rebuilt || Sp->rebuilding);
+  // all four lanes of an atom share `live`; whole quads leave together
+  if (!live) return;
+  const float cut2 = Sp->cut2;
   const float4* pos = A.pos;
   Acc f{0.f, 0.f, 0.f, 0, 0, 0};
   double eb = 0.0, ea = 0.0, ed = 0.0, ex = 0.0, en = 0.0;
 
-  // bonded terms through the incidence lists (term index * 4 + position)
   const Incidence I = A.inc[a];
   const int nb = I.counts & 0xff, na = (I.counts >> 8) & 0xff, nd = (I.counts >> 16) & 0xff;
-  for (int q = 0; q < nb; ++q) {
-    const int ent = A.inc_list[I.b_beg + q];
+  for (int t = q; t < nb; t += kLanes) {
+    const int ent = A.inc_list[I.b_beg + t];
     bond_term(pos, A.bonds[ent >> 2], ent & 3, f, kEnergy ? &eb : nullptr);
   }
-  for (int q = 0; q < na; ++q) {
-    const int ent = A.inc_list[I.a_beg + q];
+  for (int t = q; t < na; t += kLanes) {
+    const int ent = A.inc_list[I.a_beg + t];
     angle_term(pos, A.angles[ent >> 2], ent & 3, f, kEnergy ? &ea : nullptr);
   }
-  for (int q = 0; q < nd; ++q) {
-    const int ent = A.inc_list[I.d_beg + q];
+  for (int t = q; t < nd; t += kLanes) {
+    const int ent = A.inc_list[I.d_beg + t];
     dihedral_term(pos, A.dihs[ent >> 2], ent & 3, f, kEnergy ? &ed : nullptr);
   }
   f.flush();
@@ -176,9 +195,9 @@ __global__ void __launch_bounds__(128) k_force(Arena A, int64_t n_span) {
   const float4 pi = pos[a];
   // exact exceptions: no cutoff, no shift (nhs_amber_fused.cu:3316-3467)
   const int2 xr = A.ex_idx[a];
-  for (int q = 0; q < xr.y; ++q) {
-    const int j = A.ex_partner[xr.x + q];
-    const float4 par = A.ex_par[xr.x + q];
+  for (int t = q; t < xr.y; t += kLanes) {
+    const int j = A.ex_partner[xr.x + t];
+    const float4 par = A.ex_par[xr.x + t];
     const float4 pj = pos[j];
     const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
     const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
@@ -199,18 +218,19 @@ __global__ void __launch_bounds__(128) k_force(Arena A, int64_t n_span) {
   }
   f.flush();
 
-  // ordinary pairs from the interleaved neighbour row
+  // ordinary pairs: lane q walks entries q, q+4, ... of the tiled row
   const float2 li = A.lj[a];
   const float qi = pi.w;
   const int n = A.nnbr[a];
-  const int* row = A.nbr + ((int64_t)(a >> 5) * kNbrCap) * 32 + (a & 31);
+  const int* row = A.nbr + nbr_index(a, q);  // entry 4t+q is at row[32 t]
   float inv_rc = 0.f;
   if (kEnergy) inv_rc = rsqrtf(cut2);
-  for (int k0 = 0; k0 < n; k0 += 32) {
-    const int k1 = min(n, k0 + 32);
+  const int mine = n > q ? (n - q + kLanes - 1) / kLanes : 0;
+  for (int t0 = 0; t0 < mine; t0 += 32) {
+    const int t1 = min(mine, t0 + 32);
 #pragma unroll 4
-    for (int k = k0; k < k1; ++k) {
-      const int j = __ldg(row + (int64_t)k * 32);
+    for (int t = t0; t < t1; ++t) {
+      const int j = __ldg(row + (int64_t)t * 32);
       const float4 pj = __ldg(pos + j);
       const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
       const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
@@ -234,26 +254,36 @@ __global__ void __launch_bounds__(128) k_force(Arena A, int64_t n_span) {
     }
     f.flush();
   }
-  const int64_t cap = A.atom_cap;
-  A.f[a] = f.X;
-  A.f[cap + a] = f.Y;
-  A.f[2 * cap + a] = f.Z;
+  const long long X = lane_sum(f.X), Y = lane_sum(f.Y), Z = lane_sum(f.Z);
   if (kEnergy) {
-    A.pe[a] = eb;
-    A.pe[cap + a] = ea;
-    A.pe[2 * cap + a] = ed;
-    A.pe[3 * cap + a] = ex;
-    A.pe[4 * cap + a] = en;
+    eb = lane_sum(eb);
+    ea = lane_sum(ea);
+    ed = lane_sum(ed);
+    ex = lane_sum(ex);
+    en = lane_sum(en);
+  }
+  if (q == 0) {
+    const int64_t cap = A.atom_cap;
+    A.f[a] = X;
+    A.f[cap + a] = Y;
+    A.f[2 * cap + a] = Z;
+    if (kEnergy) {
+      A.pe[a] = eb;
+      A.pe[cap + a] = ea;
+      A.pe[2 * cap + a] = ed;
+      A.pe[3 * cap + a] = ex;
+      A.pe[4 * cap + a] = en;
+    }
   }
 }
 
-void launch_force(const Arena& A, int64_t n_atoms_span, bool energy, cudaStream_t st) {
+void launch_force(const Arena& A, int64_t n_atoms_span, bool energy, cudaStream_t st, bool only_rebuilt) {
   if (n_atoms_span <= 0) return;
-  const int64_t blocks = (n_atoms_span + 127) / 128;
+  const int64_t blocks = (n_atoms_span * kLanes + 127) / 128;
   if (energy)
-    k_force<true><<<(unsigned)blocks, 128, 0, st>>>(A, n_atoms_span);
+    k_force<true><<<(unsigned)blocks, 128, 0, st>>>(A, n_atoms_span, only_rebuilt ? 1 : 0);
   else
-    k_force<false><<<(unsigned)blocks, 128, 0, st>>>(A, n_atoms_span);
+    k_force<false><<<(unsigned)blocks, 128, 0, st>>>(A, n_atoms_span, only_rebuilt ? 1 : 0);
 }
 
 }  // namespace pq

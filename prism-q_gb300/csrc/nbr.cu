@@ -190,8 +190,9 @@ __global__ void __launch_bounds__(kCtlThreads) k_control_cells(Arena A, int mode
           gh[d] = fmaxf(gh[d], red_f[3 + d][w]);
         }
       }
-      // cells at least r_list·(1+1e-4) wide on every axis
-      const float edge_min = sqrtf(Sp->rlist2) * 1.0001f;
+      // cells at least r_list/2·(1+1e-4) wide on every axis; the row builder
+      // scans ±2 cells, which covers every pair within r_list
+      const float edge_min = sqrtf(Sp->rlist2) * 0.50005f;
       int nd[3];
       float ext[3];
       for (int d = 0; d < 3; ++d) {
@@ -363,13 +364,14 @@ __global__ void __launch_bounds__(kNbrThreads) k_nbr_build(Arena A, int64_t n_sp
       const int2 far = A.far[a];
       count = 0;
       bool overflow = false;
-      for (int dz = -1; dz <= 1; ++dz) {
+      const int reach = mode == 1 ? 1 : 2;  // REF27: 27 cells of 10 Å; complete: 125 cells of >= r_list/2
+      for (int dz = -reach; dz <= reach; ++dz) {
         const int z = cz + dz;
         if (z < 0 || z >= dims[2]) continue;
-        for (int dy = -1; dy <= 1; ++dy) {
+        for (int dy = -reach; dy <= reach; ++dy) {
           const int y = cy + dy;
           if (y < 0 || y >= dims[1]) continue;
-          for (int dx = -1; dx <= 1; ++dx) {
+          for (int dx = -reach; dx <= reach; ++dx) {
             const int x = cx + dx;
             if (x < 0 || x >= dims[0]) continue;
             const int c = x + y * dims[0] + z * dims[0] * dims[1];
@@ -423,13 +425,17 @@ __global__ void __launch_bounds__(kNbrThreads) k_nbr_build(Arena A, int64_t n_sp
   }
   if (lane == 0) cnt[warp] = count;
   __syncthreads();
-  // coalesced write of the interleaved rows: element (k, atom w) -> ((g*cap + k)*32 + w)
+  // coalesced write of the tiled rows: the block's 32 atoms are four groups of
+  // eight; consecutive threads write consecutive words of nbr_index order
   int maxc = 0;
   for (int w = 0; w < 32; ++w) maxc = max(maxc, cnt[w]);
-  int* out = A.nbr + (g * kNbrCap) * 32;
-  for (int idx = threadIdx.x; idx < maxc * 32; idx += kNbrThreads) {
-    const int k = idx >> 5, w = idx & 31;
-    if (k < cnt[w]) out[idx] = rows[w * kNbrCap + k];
+  const int lines = (maxc + 3) >> 2;  // 4-entry lines per atom
+  int* out = A.nbr + g * 4 * (int64_t)kNbrCap * 8;
+  for (int idx = threadIdx.x; idx < 4 * lines * 32; idx += kNbrThreads) {
+    const int gi = idx / (lines * 32), rem = idx - gi * lines * 32;
+    const int t = rem >> 5, within = rem & 31;
+    const int w = gi * 8 + (within >> 2), k = 4 * t + (within & 3);
+    if (k < cnt[w]) out[(int64_t)gi * kNbrCap * 8 + t * 32 + within] = rows[w * kNbrCap + k];
   }
 }
 

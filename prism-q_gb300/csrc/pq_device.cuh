@@ -13,6 +13,14 @@
 namespace pq {
 
 constexpr int kNbrCap = 1024;     // neighbour row capacity per atom
+constexpr int kLanes = 4;         // threads per atom in the force kernel (fixed: results depend on it)
+
+// Row storage is tiled for the force kernel's warp shape (8 atoms x 4 lanes):
+// entry k of atom a lives at group (a/8), line k/4, slot (a%8)*4 + k%4, so a
+// warp's 32 index loads for one iteration are one contiguous 128-byte line.
+__host__ __device__ __forceinline__ int64_t nbr_index(int64_t a, int k) {
+  return ((a >> 3) * kNbrCap + (k & ~3)) * 8 + ((a & 7) << 2) + (k & 3);
+}
 constexpr int kRefCellCap = 512;  // REF27 cell capacity (MAX_ATOMS_PER_CELL)
 constexpr int kRefMaxDim = 32;    // REF27 cells per axis (MAX_CELLS_PER_DIM)
 
@@ -114,7 +122,7 @@ struct Arena {
   // constraint units
   Unit* units = nullptr;
   // lists
-  int* nbr = nullptr;   // interleaved rows: ((a>>5)*kNbrCap + k)*32 + (a&31)
+  int* nbr = nullptr;   // tiled rows, see nbr_index()
   int* nnbr = nullptr;  // row lengths
   int* cell_start = nullptr;  // per system: cell_cap+1 entries
   int* cell_atoms = nullptr;  // per atom (sorted by cell)
@@ -138,7 +146,8 @@ void launch_control_cells(const Arena& A, int n_sys, int mode, int nbr_mode_over
                           cudaStream_t st);
 void launch_nbr_build(const Arena& A, int64_t n_atoms_span, int exclude_exceptions,
                       cudaStream_t st);
-void launch_force(const Arena& A, int64_t n_atoms_span, bool energy, cudaStream_t st);
+void launch_force(const Arena& A, int64_t n_atoms_span, bool energy, cudaStream_t st,
+                  bool only_rebuilt = false);
 void launch_integrate(const Arena& A, int64_t n_units_span, int mode, cudaStream_t st);
 void launch_debug_phases(const Arena& A, int64_t n_units_span, int set, long long step,
                          cudaStream_t st);

@@ -1,0 +1,262 @@
+"""GPU parity: the CUDA path through the C ABI against the CPU oracle and the
+reference's golden pair sets.
+
+Bars (stated per test):
+  * neighbour pair sets: bit-exact (REF27 vs the reference scheme, COMPLETE vs
+    brute force) — integer/index work keeps its arithmetic;
+  * forces: relative RMS <= 1e-5 against the FP64 oracle; potential energy
+    within 1e-6 relative;
+  * integrator phases: bit-exact against the oracle given the device forces;
+  * whole steps: bit-exact against the oracle's phases fed the device forces.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import rel_rms
+
+pytestmark = pytest.mark.gpu
+
+FORCE_RTOL = 1e-5
+ENERGY_RTOL = 1e-6
+
+
+def _oracle(orc, topo, params, **kw):
+    return orc.OracleSystem(topo.struct(), dt=params.dt, temperature=params.temperature, gamma=params.gamma,
+                            cutoff=params.cutoff, max_iter=params.max_constraint_iter,
+                            com_interval=params.com_interval, seed=params.seed, stream=params.stream, **kw)
+
+
+@pytest.mark.parametrize("case", ["synthetic_600", "drift_25x", "cloud_2000"])
+def test_pair_sets_match_reference_golden(gpu, golden, case):
+    import hashlib
+
+    pos, gpos = golden[f"{case}/pos"], golden[f"{case}/grid_pos"]
+    topo = gpu.Topology.point_cloud(gpos)
+    eng = gpu.NhsAmberFusedEngine(topo, gpu.Params())
+    eng.set_positions(pos)  # the reference grid stays fixed at the construction positions
+    sha = lambda a: hashlib.sha256(np.ascontiguousarray(a, dtype="<i4").tobytes()).hexdigest()
+    ref = eng.build_neighbors(gpu.NLIST_REF27)
+    assert len(ref) == golden[f"{case}/counts"][1]
+    assert sha(ref) == str(golden[f"{case}/kept_sha256"])
+    comp = eng.build_neighbors(gpu.NLIST_COMPLETE)
+    assert len(comp) == golden[f"{case}/counts"][0]
+    assert sha(comp) == str(golden[f"{case}/brute_sha256"])
+    eng.close()
+
+
+def test_pair_sets_polyala_with_exclusions(gpu, orc, ala250):
+    p = gpu.Params()
+    eng = gpu.NhsAmberFusedEngine(ala250, p)
+    o = _oracle(orc, ala250, p)
+    off, lst = o.ref_exclusions()
+    want_ref, _ = orc.pairs_ref27(ala250.positions, ala250.positions, 144.0, off, lst)
+    want_all = orc.pairs_brute(ala250.positions, 144.0, off, lst)
+    got_ref = eng.build_neighbors(gpu.NLIST_REF27)
+    got_all = eng.build_neighbors(gpu.NLIST_COMPLETE)
+    assert np.array_equal(got_ref, want_ref)
+    assert np.array_equal(got_all, want_all)
+    # REF27 ⊂ COMPLETE, and every pair the reference scheme misses lies beyond 10 Å
+    s_ref = set(map(tuple, got_ref.tolist()))
+    s_all = set(map(tuple, got_all.tolist()))
+    assert s_ref <= s_all
+    missed = np.array(sorted(s_all - s_ref)).reshape(-1, 2)
+    if len(missed):
+        d = ala250.positions[missed[:, 0]].astype(np.float64) - ala250.positions[missed[:, 1]]
+        assert (np.linalg.norm(d, axis=1) > 10.0).all()
+    eng.close()
+
+
+@pytest.mark.parametrize("nchains,nres,box", [(1, 40, 0.0), (1, 250, 0.0), (3, 60, 70.0)])
+def test_forces_and_energy_vs_fp64_oracle(gpu, orc, nchains, nres, box):
+    topo = gpu.Topology.polyala(nchains, nres, seed=7, box_edge=box)
+    p = gpu.Params()
+    eng = gpu.NhsAmberFusedEngine(topo, p)
+    pe, f, fx = eng.compute_forces()
+    o = _oracle(orc, topo, p)
+    f64, e64 = o.forces_f64()
+    assert rel_rms(f, f64) <= FORCE_RTOL
+    assert abs(pe - e64.sum()) <= ENERGY_RTOL * abs(e64).sum()
+    comp = eng.energy_components()
+    for k in range(5):
+        assert abs(comp[k] - e64[k]) <= ENERGY_RTOL * max(abs(e64[k]), 1.0), (k, comp[k], e64[k])
+    # float and fixed-point outputs agree: f = fixed * 2^-32
+    assert np.array_equal(f, (fx.astype(np.float32) * np.float32(2.0 ** -32)))
+    # the FP32 restatement of the reference gather lands within the same bar
+    f32, _ = o.forces_ref_f32()
+    assert rel_rms(f, f32) <= FORCE_RTOL
+    eng.close()
+
+
+def test_forces_are_bitwise_deterministic(gpu, ala250):
+    eng = gpu.NhsAmberFusedEngine(ala250, gpu.Params())
+    a = eng.compute_forces()[2]
+    b = eng.compute_forces()[2]
+    eng2 = gpu.NhsAmberFusedEngine(ala250, gpu.Params())
+    c = eng2.compute_forces()[2]
+    assert np.array_equal(a, b) and np.array_equal(a, c)
+    eng.close()
+    eng2.close()
+
+
+@pytest.mark.parametrize("gamma", [1.0, 0.0])
+def test_phase_sets_bit_exact(gpu, orc, ala40, gamma):
+    p = gpu.Params(gamma=gamma)
+    eng = gpu.NhsAmberFusedEngine(ala40, p)
+    o = _oracle(orc, ala40, p)
+    for step in (0, 3, 101):
+        x, v = eng.get_positions(), eng.get_velocities()
+        _, _, fx = eng.compute_forces()
+        o.set_state(x, v)
+        eng.debug_phases(gpu.PHASES_PRE, step)
+        assert o.phases(1, fx, step) == 0
+        xg, vg = eng.get_positions(), eng.get_velocities()
+        xo, vo = o.get_state()
+        assert np.array_equal(xg, xo) and np.array_equal(vg, vo)
+        _, _, fx = eng.compute_forces()
+        eng.debug_phases(gpu.PHASES_POST, step)
+        assert o.phases(2, fx, step) == 0
+        xg, vg = eng.get_positions(), eng.get_velocities()
+        xo, vo = o.get_state()
+        assert np.array_equal(xg, xo) and np.array_equal(vg, vo)
+    eng.close()
+
+
+@pytest.mark.parametrize("start_step", [0, 7, 100])
+def test_full_step_bit_exact_with_device_forces(gpu, orc, ala40, start_step):
+    """One production step (fused kernels, graph) equals the oracle's reference
+    phase order fed the device forces F(x_n) and F(x_n+1); start 100 includes
+    the COM removal at the start of the step."""
+    p = gpu.Params()
+    eng = gpu.NhsAmberFusedEngine(ala40, p)
+    eng.step(3)  # leave the initial state
+    eng.set_timestep(start_step)
+    x, v = eng.get_positions(), eng.get_velocities()
+    _, _, f_n = eng.compute_forces()
+    eng.step(1)
+    _, _, f_np1 = eng.compute_forces()
+    o = _oracle(orc, ala40, p)
+    o.set_state(x, v)
+    if start_step > 0 and start_step % p.com_interval == 0:
+        o.com_remove()
+    assert o.phases(1, f_n, start_step) == 0
+    xo_mid, _ = o.get_state()
+    assert o.phases(2, f_np1, start_step) == 0
+    xg, vg = eng.get_positions(), eng.get_velocities()
+    xo, vo = o.get_state()
+    assert np.array_equal(xg, xo_mid) and np.array_equal(xg, xo)
+    assert np.array_equal(vg, vo)
+    assert eng.timestep == start_step + 1
+    eng.close()
+
+
+def test_trajectory_tracks_reference_cpu_path(gpu, orc, ala40):
+    """50 steps of the GPU step vs the oracle's reference step loop (its own FP32
+    forces, per-step REF27 list, same injected noise).  The two force
+    evaluations differ at ~1e-6 relative, and MD amplifies that difference, so
+    the stated tolerance grows with time: after 10 steps max |dx| < 2e-4 Å;
+    after 50 steps RMS |dx| < 2e-3 Å and max |dx| < 1e-2 Å."""
+    p = gpu.Params()
+    eng = gpu.NhsAmberFusedEngine(ala40, p)
+    x, v = eng.get_positions(), eng.get_velocities()
+    o = _oracle(orc, ala40, p)
+    o.set_state(x, v)
+    eng.step(10)
+    assert o.run(10) == 0
+    d = eng.get_positions().astype(np.float64) - o.get_state()[0]
+    assert np.abs(d).max() < 2e-4
+    eng.step(40)
+    assert o.run(40) == 0
+    d = eng.get_positions().astype(np.float64) - o.get_state()[0]
+    assert np.sqrt((d ** 2).sum(1).mean()) < 2e-3
+    assert np.abs(d).max() < 1e-2
+    eng.close()
+
+
+def _temperature(v, m, n_constraints):
+    ke = 0.5 * (m[:, None] * v.astype(np.float64) ** 2).sum() / 418.4
+    dof = 3 * len(m) - n_constraints - 3
+    return 2.0 * ke / (dof * 0.001987204)
+
+
+def test_thousand_step_statistics_match_reference_cpu_path(gpu, orc, ala40):
+    """1,000 steps (4 ps) of the GPU step and of the oracle's reference step loop
+    from the same state and noise: trajectories decorrelate, so the comparison
+    is statistical — mean kinetic temperature over steps 500-1000 within 5% of
+    each other and of the 300 K bath, mean potential energy within 3% of the
+    mean total |PE| scale."""
+    p = gpu.Params()
+    eng = gpu.NhsAmberFusedEngine(ala40, p)
+    o = _oracle(orc, ala40, p)
+    o.set_state(eng.get_positions(), eng.get_velocities())
+    ncon = int(sum(int(c["n_hydrogens"]) for c in ala40.clusters))
+    m = ala40.masses.astype(np.float64)
+    tg, to, eg, eo = [], [], [], []
+    for blk in range(20):
+        eng.step(50)
+        assert o.run(50) == 0
+        if blk >= 10:
+            tg.append(_temperature(eng.get_velocities(), m, ncon))
+            to.append(_temperature(o.get_state()[1], m, ncon))
+            eg.append(eng.compute_forces()[0])
+            eo.append(o.forces_ref_f32()[1].sum())
+    tg, to = np.mean(tg), np.mean(to)
+    assert abs(tg - to) / 300.0 < 0.05
+    assert abs(tg - 300.0) / 300.0 < 0.08 and abs(to - 300.0) / 300.0 < 0.08
+    scale = np.mean(np.abs(eo))
+    assert abs(np.mean(eg) - np.mean(eo)) / scale < 0.03
+    eng.close()
+
+
+def test_repeat_runs_are_bit_identical(gpu, ala250):
+    a = gpu.NhsAmberFusedEngine(ala250, gpu.Params())
+    b = gpu.NhsAmberFusedEngine(ala250, gpu.Params())
+    a.step(137)
+    b.step(60)
+    b.step(77)  # different call split, same trajectory
+    assert np.array_equal(a.get_positions(), b.get_positions())
+    assert np.array_equal(a.get_velocities(), b.get_velocities())
+    a.close()
+    b.close()
+
+
+def test_constraints_hold_along_the_trajectory(gpu, ala250):
+    eng = gpu.NhsAmberFusedEngine(ala250, gpu.Params())
+    for _ in range(5):
+        eng.step(40)
+        x = eng.get_positions().astype(np.float64)
+        for c in ala250.clusters:
+            for h, L in zip(c["hydrogen_atoms"], c["bond_lengths"]):
+                if h >= 0:
+                    r2 = ((x[h] - x[c["central_atom"]]) ** 2).sum()
+                    # SHAKE tolerance of the reference: |r^2 - L^2| / L^2 <= 1e-4 (f32 residual)
+                    assert abs(r2 - L * L) / (L * L) <= 1.2e-4
+    eng.close()
+
+
+def test_shake_nonconvergence_is_reported_not_trapped(gpu, ala40):
+    p = gpu.Params(max_constraint_iter=1, temperature=600.0)
+    eng = gpu.NhsAmberFusedEngine(ala40, p)
+    with pytest.raises(gpu.PrismQError) as e:
+        eng.step(50)
+    assert e.value.status in (7, 8)  # E_SHAKE / E_RATTLE; the context stays usable
+    eng2 = gpu.NhsAmberFusedEngine(ala40, gpu.Params())
+    eng2.step(5)
+    eng.close()
+    eng2.close()
+
+
+def test_invalid_topology_rejected_on_host(gpu, ala40):
+    bad = gpu.Topology(ala40.positions, ala40.masses, ala40.charges, ala40.lj_sigma, ala40.lj_epsilon,
+                       ala40.bonds.copy(), ala40.angles, ala40.dihedrals, ala40.exceptions,
+                       ala40.exclusion_offsets, ala40.exclusions, ala40.clusters.copy())
+    bad.clusters["inv_mass_h"][0] *= 1.5  # inconsistent with the hydrogen's mass
+    with pytest.raises(gpu.PrismQError) as e:
+        gpu.NhsAmberFusedEngine(bad, gpu.Params())
+    assert e.value.status == 1
+    bad2 = gpu.Topology(ala40.positions, ala40.masses, ala40.charges, ala40.lj_sigma, ala40.lj_epsilon,
+                        ala40.bonds.copy())
+    bad2.bonds["j"][0] = ala40.n_atoms + 5
+    with pytest.raises(gpu.PrismQError):
+        gpu.NhsAmberFusedEngine(bad2, gpu.Params())
