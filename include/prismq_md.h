@@ -250,6 +250,34 @@ prismq_status prismq_batch_get_state_all(prismq_batch* b, float* xyz, float* vxy
 prismq_status prismq_batch_run_timed(prismq_batch* b, int64_t n_steps, float* total_ms, float* force_ms);
 int32_t prismq_batch_resident_systems(const prismq_batch* b);
 
+/* ---- neighbour rows without device allocation ----
+ *
+ * No counterpart in the reference: it serves callers that cannot allocate
+ * device memory while they run — for example a serving process that reserves
+ * its whole HBM budget for job arenas at start-up, or a host loop whose
+ * allocator policy forbids cudaMalloc/cudaFree after start-up because they
+ * synchronise the device and fragment memory.
+ *
+ * Builds the complete neighbour rows of a point set (every j != i with
+ * (dx*dx + dy*dy) + dz*dz <= list_radius^2 in FP32, the batched builder's
+ * complete-mode rule) into caller-owned DEVICE buffers:
+ *   d_xyz     device float[3*n_atoms] positions (Å)
+ *   d_rows    device int32[n_atoms*row_cap]; row i holds its neighbours
+ *   d_counts  device int32[n_atoms]; row lengths (-1 for a row that overflowed)
+ *   stream    a cudaStream_t (NULL for the default stream)
+ * Limits: 1 <= n_atoms <= 65536, 1 <= row_cap <= 1024, at most 512 atoms in a
+ * cell (cells are at least list_radius/2 wide); larger sizes are rejected with
+ * PRISMQ_E_CAPACITY before any GPU work.  The call calls no cudaMalloc or
+ * cudaFree: its cell lists live in one fixed file-scope device array (about
+ * 0.8 MB) that every GPU loading the library keeps until the process exits.
+ * The first call on a device looks up that array's device address (set-up
+ * work; make it before any stream capture).  Every call reuses the same array,
+ * so calls that overlap on the GPU race and must be serialised by the caller.
+ * The call returns after the stream has finished the work. */
+prismq_status prismq_neighbor_rows_noalloc(const float* d_xyz, int32_t n_atoms, float list_radius,
+                                           int32_t row_cap, int32_t* d_rows, int32_t* d_counts,
+                                           void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -30,6 +30,7 @@ UNITS = {
     "force.cu": [],
     "integrate.cu": ["--fmad=false"],
     "nbr.cu": ["--fmad=false"],
+    "noalloc.cu": ["--fmad=false"],
     "topology.cpp": [],
 }
 

@@ -39,6 +39,11 @@ static prismq_status fail(prismq_status st, const std::string& msg) {
   return st;
 }
 
+namespace pq {
+// Lets entry points in other translation units report through prismq_last_error().
+void set_last_error(const std::string& msg) { g_err = msg; }
+}  // namespace pq
+
 #define PQ_CK(x)                                                                             \
   do {                                                                                       \
     cudaError_t e_ = (x);                                                                    \
