@@ -55,6 +55,8 @@ def args_parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--equil", type=int, default=400,
+                    help="MD steps run on the freshly grown systems before warm-up (equilibration)")
     return ap.parse_args()
 
 
@@ -267,7 +269,10 @@ def run_ours(args, pq, rank, world):
     slots = []
     for i, t in zip(mine, topos):
         slots.append(batch.add_system(t, pq.Params(stream=i)))
+    if args.equil > 0:
+        batch.step(args.equil)  # leave the transient right after growth
     batch.step(max(args.warmup, 3))
+    rebuilds0 = sum(batch.counters(s)[1] for s in slots)
     # pair statistics at the warmed-up positions
     stats = []
     for s, t in zip(slots, topos):
@@ -283,18 +288,23 @@ def run_ours(args, pq, rank, world):
     barrier(world)
     clocks.start()
     total_ms = ctypes.c_float()
-    force_ms = (ctypes.c_float * args.steps)()
+    phase_ms = (ctypes.c_float * (4 * args.steps))()
     rc = pq.load().prismq_batch_run_timed(batch.h, args.steps, ctypes.addressof(total_ms),
-                                          ctypes.addressof(force_ms))
+                                          ctypes.addressof(phase_ms))
     if rc:
         raise pq.PrismQError(rc, pq.load().prismq_last_error().decode())
     clk = clocks.stop()
     barrier(world)
     launches = pq.kernel_launches() - launches0
+    # list builds during the timed region (the run advances steps+1 steps)
+    builds = sum(batch.counters(s)[1] for s in slots) - rebuilds0
+    steps_per_build = len(slots) * (args.steps + 1) / max(builds, 1)
     t_max = max_over_ranks(total_ms.value / 1e3, world)
     total_atoms = sum_over_ranks(float(atoms), world)
     value = total_atoms * args.steps / t_max
-    f_avg_ms = statistics.mean(force_ms[i] for i in range(args.steps))
+    kernels = ["k_control_cells", "k_nbr_build", "k_force", "k_integrate"]
+    phase_avg = {k: statistics.mean(phase_ms[4 * i + p] for i in range(args.steps)) for p, k in enumerate(kernels)}
+    f_avg_ms = phase_avg["k_force"]
     achieved = flops_launch / (f_avg_ms / 1e3) / 1e12
     # ---------------- e2e through the C ABI with pinned host buffers
     span = int(pq.load().prismq_batch_atom_span(batch.h))
@@ -366,7 +376,8 @@ def run_ours(args, pq, rank, world):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded poly-alanine systems; no dataset)",
         "config": {"workload": args.workload, "systems": len(specs), "atoms_total": int(total_atoms),
-                   "atoms_rank0": atoms, "p10_per_atom": p10_mean,
+                   "atoms_rank0": atoms, "p10_per_atom": p10_mean, "equilibration_steps": args.equil,
+                   "steps_per_list_build": steps_per_build, "force_launch_shape": batch.tuning(),
                    "parallelism": f"independent systems sharded over {world} GPU(s)",
                    "l2": "inputs larger than L2 (neighbour rows ~4 KiB/atom, re-read every step)"},
         "e2e": {"value": e2e_value, "unit": "atom-steps/s", "h2d_bytes_per_step": 24 * span,
@@ -374,7 +385,8 @@ def run_ours(args, pq, rank, world):
         "plain": None if plain_value is None else {"value": plain_value, "unit": "atom-steps/s",
                                                    "batched_over_plain": value / plain_value,
                                                    "sample": "8 stratified systems run alone, 200 steps each"},
-        "roofline": roof, "hbm": hbm, "gpu_launches": int(launches), "clocks": clk, "cpu_baseline": cpu,
+        "roofline": roof, "hbm": hbm, "kernel_avg_ms": phase_avg, "gpu_launches": int(launches), "clocks": clk,
+        "cpu_baseline": cpu,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

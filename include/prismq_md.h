@@ -233,6 +233,13 @@ prismq_status prismq_batch_set_state(prismq_batch* b, int32_t slot, const float*
                                      const float* vxyz);
 prismq_status prismq_batch_get_step(prismq_batch* b, int32_t slot, int64_t* step);
 prismq_status prismq_batch_status(prismq_batch* b, int32_t slot);
+/* The autotuner's choice for the batch's force kernel: out[0] = variant
+ * (-1 before the first step), out[1] = threads per block, out[2] = minimum
+ * resident blocks per SM given to the register allocator.  The launch shape
+ * does not change results. */
+prismq_status prismq_batch_tuning(prismq_batch* b, int32_t out[3]);
+/* out[0] = steps taken, out[1] = neighbour-list builds so far. */
+prismq_status prismq_batch_counters(prismq_batch* b, int32_t slot, int64_t out[2]);
 prismq_status prismq_batch_energy(prismq_batch* b, int32_t slot, double out[6]);
 int64_t prismq_batch_resident_atoms(const prismq_batch* b);
 /* Whole-arena state transfer: float[3*span] in arena atom order (span =
@@ -246,8 +253,10 @@ prismq_status prismq_batch_set_state_all(prismq_batch* b, const float* xyz, cons
 prismq_status prismq_batch_get_state_all(prismq_batch* b, float* xyz, float* vxyz);
 /* Advance every resident system by n_steps+1 steps, of which n_steps are
  * captured in one CUDA graph and timed on the device: total_ms covers those
- * n_steps, force_ms[i] (optional, n_steps entries) the force launch of step i. */
-prismq_status prismq_batch_run_timed(prismq_batch* b, int64_t n_steps, float* total_ms, float* force_ms);
+ * n_steps; phase_ms (optional, 4*n_steps entries) holds, for step i at
+ * [4i..4i+3], the device time of its control, neighbour-row, force and
+ * integrate launches (events recorded between the launches). */
+prismq_status prismq_batch_run_timed(prismq_batch* b, int64_t n_steps, float* total_ms, float* phase_ms);
 int32_t prismq_batch_resident_systems(const prismq_batch* b);
 
 /* ---- neighbour rows without device allocation ----

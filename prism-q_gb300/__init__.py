@@ -149,6 +149,8 @@ def load() -> ctypes.CDLL:
         "prismq_batch_set_state_all": (I, [P, P, P]),
         "prismq_batch_get_state_all": (I, [P, P, P]),
         "prismq_batch_run_timed": (I, [P, i64, P, P]),
+        "prismq_batch_counters": (I, [P, ctypes.c_int32, P]),
+        "prismq_batch_tuning": (I, [P, P]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(L, name)
@@ -446,6 +448,18 @@ class Batch:
 
     def status(self, slot: int) -> int:
         return load().prismq_batch_status(self.h, slot)
+
+    def tuning(self) -> dict:
+        """The autotuner's force-kernel launch shape for this batch."""
+        out = np.zeros(3, np.int32)
+        _check(load().prismq_batch_tuning(self.h, _ptr(out)))
+        return {"variant": int(out[0]), "block": int(out[1]), "min_blocks_per_sm": int(out[2])}
+
+    def counters(self, slot: int) -> tuple[int, int]:
+        """(steps taken, neighbour-list builds) of one system."""
+        out = np.zeros(2, np.int64)
+        _check(load().prismq_batch_counters(self.h, slot, _ptr(out)))
+        return int(out[0]), int(out[1])
 
     def energy(self, slot: int) -> np.ndarray:
         out = np.zeros(6, np.float64)

@@ -15,6 +15,7 @@
 // CUDA graph:  control+cells (per system) → neighbour rows → forces →
 // integrate (post-phases of this step fused with pre-phases of the next).
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <atomic>
@@ -305,7 +306,11 @@ prismq_status lower_topology(const prismq_topology* T, Lowered* L) {
       U.nh = 0;
       L->units.push_back(U);
     }
-  std::stable_sort(L->units.begin(), L->units.end(), [](const Unit& x, const Unit& y) { return x.a[0] < y.a[0]; });
+  // Units with the same hydrogen count sit together, so a warp of the
+  // integrator runs one control path (no per-atom or constraint divergence).
+  std::stable_sort(L->units.begin(), L->units.end(), [](const Unit& x, const Unit& y) {
+    return x.nh != y.nh ? x.nh > y.nh : x.a[0] < y.a[0];
+  });
   // ---- reference grid (CELL_SIZE 10 Å, one cell of padding, ≤ 32 per axis) ----
   float mn[3] = {3.4e38f, 3.4e38f, 3.4e38f}, mx[3] = {-3.4e38f, -3.4e38f, -3.4e38f};
   for (int a = 0; a < n; ++a)
@@ -469,6 +474,8 @@ struct prismq_batch {
   bool graph_dirty = true;
   int64_t atom_span = 0, unit_span = 0;
   int sys_span = 0;
+  int force_variant = -1;  // autotuned launch shape of the force kernel
+  int64_t tuned_span = -1;
   double* d_energy = nullptr;
   float* d_stage = nullptr;
   float* d_stage2 = nullptr;
@@ -478,7 +485,7 @@ struct prismq_batch {
     if (gexec) cudaGraphExecDestroy(gexec);
     void* ptrs[] = {A.pos, A.vel, A.lj, A.xref, A.f, A.pe, A.atom_sys, A.mask_all, A.mask_ref, A.far,
                     A.far_list, A.inc, A.inc_list, A.ex_idx, A.ex_partner, A.ex_par, A.bonds, A.angles,
-                    A.dihs, A.units, A.nbr, A.nnbr, A.cell_start, A.cell_atoms, A.atom_cell, A.sys,
+                    A.dihs, A.units, A.nbr, A.nnbr, A.cell_start, A.cell_atoms, A.atom_cell, A.work, A.work_ctl, A.sys,
                     d_energy, d_stage, d_stage2};
     for (void* p : ptrs)
       if (p) cudaFree(p);
@@ -506,10 +513,44 @@ struct prismq_batch {
   void enqueue_step_body() {
     launch_control_cells(A, sys_span, kCtlStep, -1, st);
     launch_nbr_build(A, atom_span, 1, st);
-    launch_force(A, atom_span, false, st);
+    launch_force(A, atom_span, false, st, false, force_variant);
+  }
+
+  // Autotuner: time every force-kernel launch shape on the resident batch
+  // (three launches each, CUDA events) and keep the fastest.  The shapes give
+  // identical forces, so the choice affects speed only.
+  prismq_status tune_force() {
+    if (force_variant >= 0 && tuned_span == atom_span) return PRISMQ_OK;
+    cudaEvent_t e0, e1;
+    PQ_CK(cudaEventCreate(&e0));
+    PQ_CK(cudaEventCreate(&e1));
+    float best = 3.4e38f;
+    int pick = 0;
+    for (int v = 0; v < force_variant_count(); ++v) {
+      launch_force(A, atom_span, false, st, false, v);
+      PQ_CK(cudaEventRecord(e0, st));
+      for (int r = 0; r < 3; ++r) launch_force(A, atom_span, false, st, false, v);
+      PQ_CK(cudaEventRecord(e1, st));
+      PQ_CK(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      PQ_CK(cudaEventElapsedTime(&ms, e0, e1));
+      if (ms < best) {
+        best = ms;
+        pick = v;
+      }
+      g_launches += 4;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    PQ_CK(cudaGetLastError());
+    force_variant = pick;
+    tuned_span = atom_span;
+    return PRISMQ_OK;
   }
 
   prismq_status ensure_graph() {
+    prismq_status trc = tune_force();
+    if (trc != PRISMQ_OK) return trc;
     if (!graph_dirty && gexec) return PRISMQ_OK;
     if (gexec) {
       cudaGraphExecDestroy(gexec);
@@ -569,38 +610,46 @@ struct prismq_batch {
 
   // n steady steps captured in one graph with an event pair around every force
   // launch; head and tail phases run outside the timed graph.
-  prismq_status run_timed(int64_t n, float* total_ms, float* force_ms) {
+  // phase_ms (optional, 4*n entries): for step i the device time of the
+  // control, neighbour-row, force and integrate launches, from events recorded
+  // between consecutive launches inside the graph.
+  prismq_status run_timed(int64_t n, float* total_ms, float* phase_ms) {
     if (n <= 0 || sys_span == 0) return fail(PRISMQ_E_INVALID, "nothing to time");
     prismq_status rc = prime_if_needed();
     if (rc != PRISMQ_OK) return rc;
-    std::vector<cudaEvent_t> ev(2 * n + 2);
+    if ((rc = tune_force()) != PRISMQ_OK) return rc;
+    std::vector<cudaEvent_t> ev(4 * n + 1);
     for (auto& e : ev) PQ_CK(cudaEventCreate(&e));
     launch_integrate(A, unit_span, kIntPre, st);
     g_launches += 1;
     cudaGraph_t g;
     cudaGraphExec_t ge = nullptr;
     PQ_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    cudaEventRecordWithFlags(ev[0], st, cudaEventRecordExternal);
     for (int64_t i = 0; i < n; ++i) {
+      cudaEventRecordWithFlags(ev[4 * i + 0], st, cudaEventRecordExternal);
       launch_control_cells(A, sys_span, kCtlStep, -1, st);
+      cudaEventRecordWithFlags(ev[4 * i + 1], st, cudaEventRecordExternal);
       launch_nbr_build(A, atom_span, 1, st);
-      cudaEventRecordWithFlags(ev[2 + 2 * i], st, cudaEventRecordExternal);
-      launch_force(A, atom_span, false, st);
-      cudaEventRecordWithFlags(ev[3 + 2 * i], st, cudaEventRecordExternal);
+      cudaEventRecordWithFlags(ev[4 * i + 2], st, cudaEventRecordExternal);
+      launch_force(A, atom_span, false, st, false, force_variant);
+      cudaEventRecordWithFlags(ev[4 * i + 3], st, cudaEventRecordExternal);
       launch_integrate(A, unit_span, kIntBoth, st);
     }
-    cudaEventRecordWithFlags(ev[1], st, cudaEventRecordExternal);
+    cudaEventRecordWithFlags(ev[4 * n], st, cudaEventRecordExternal);
     PQ_CK(cudaStreamEndCapture(st, &g));
     cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
     cudaGraphDestroy(g);
     PQ_CK(e);
     PQ_CK(cudaStreamSynchronize(st));
-    PQ_CK(cudaGraphLaunch(ge, st));
+    nvtxRangePushA("prismq_timed");  // profilers can restrict capture to this range
+    cudaError_t le = cudaGraphLaunch(ge, st);
+    nvtxRangePop();
+    PQ_CK(le);
     g_launches += 4 * n;
     PQ_CK(cudaStreamSynchronize(st));
-    PQ_CK(cudaEventElapsedTime(total_ms, ev[0], ev[1]));
-    if (force_ms)
-      for (int64_t i = 0; i < n; ++i) PQ_CK(cudaEventElapsedTime(&force_ms[i], ev[2 + 2 * i], ev[3 + 2 * i]));
+    PQ_CK(cudaEventElapsedTime(total_ms, ev[0], ev[4 * n]));
+    if (phase_ms)
+      for (int64_t i = 0; i < 4 * n; ++i) PQ_CK(cudaEventElapsedTime(&phase_ms[i], ev[i], ev[i + 1]));
     cudaGraphExecDestroy(ge);
     for (auto& x : ev) cudaEventDestroy(x);
     enqueue_step_body();
@@ -685,6 +734,8 @@ prismq_status batch_alloc(prismq_batch* B, int64_t atom_cap, int sys_cap, int64_
   PQ_ALLOC(A.cell_start, A.cell_cap);
   PQ_ALLOC(A.cell_atoms, atom_cap);
   PQ_ALLOC(A.atom_cell, atom_cap);
+  PQ_ALLOC(A.work, atom_cap / 8 + sys_cap + 1);
+  PQ_ALLOC(A.work_ctl, 4);
   PQ_ALLOC(A.sys, sys_cap);
   PQ_ALLOC(B->d_energy, 6 * (int64_t)sys_cap);
   PQ_ALLOC(B->d_stage, 3 * atom_cap);
@@ -692,6 +743,7 @@ prismq_status batch_alloc(prismq_batch* B, int64_t atom_cap, int sys_cap, int64_
 #undef PQ_ALLOC
   PQ_CK(cudaMemsetAsync(A.sys, 0, sizeof(SysDev) * sys_cap, B->st));
   PQ_CK(cudaMemsetAsync(A.nnbr, 0, sizeof(int) * atom_cap, B->st));
+  PQ_CK(cudaMemsetAsync(A.work_ctl, 0, sizeof(int) * 4, B->st));
   PQ_CK(cudaMemsetAsync(A.f, 0, sizeof(long long) * 3 * atom_cap, B->st));
   PQ_CK(cudaMemsetAsync(A.pe, 0, sizeof(double) * 5 * atom_cap, B->st));
   k_fill_int<<<(unsigned)((atom_cap + 255) / 256), 256, 0, B->st>>>(A.atom_sys, -1, atom_cap);
@@ -1064,6 +1116,25 @@ prismq_status prismq_batch_get_step(prismq_batch* b, int32_t slot, int64_t* step
   return PRISMQ_OK;
 }
 
+prismq_status prismq_batch_tuning(prismq_batch* b, int32_t out[3]) {
+  if (!b || !out) return fail(PRISMQ_E_INVALID, "NULL argument");
+  out[0] = b->force_variant;
+  out[1] = out[2] = 0;
+  if (b->force_variant >= 0) force_variant_shape(b->force_variant, &out[1], &out[2]);
+  return PRISMQ_OK;
+}
+
+prismq_status prismq_batch_counters(prismq_batch* b, int32_t slot, int64_t out[2]) {
+  prismq_status rc = check_slot(b, slot);
+  if (rc != PRISMQ_OK) return rc;
+  if (!out) return fail(PRISMQ_E_INVALID, "out is NULL");
+  rc = b->sync_sys_from_device();
+  if (rc != PRISMQ_OK) return rc;
+  out[0] = b->h_sys[slot].step;
+  out[1] = b->h_sys[slot].n_rebuilds;
+  return PRISMQ_OK;
+}
+
 prismq_status prismq_batch_status(prismq_batch* b, int32_t slot) {
   prismq_status rc = check_slot(b, slot);
   if (rc != PRISMQ_OK) return rc;
@@ -1081,9 +1152,9 @@ prismq_status prismq_batch_energy(prismq_batch* b, int32_t slot, double out[6]) 
   return PRISMQ_OK;
 }
 
-prismq_status prismq_batch_run_timed(prismq_batch* b, int64_t n_steps, float* total_ms, float* force_ms) {
+prismq_status prismq_batch_run_timed(prismq_batch* b, int64_t n_steps, float* total_ms, float* phase_ms) {
   if (!b || !total_ms) return fail(PRISMQ_E_INVALID, "NULL argument");
-  return b->run_timed(n_steps, total_ms, force_ms);
+  return b->run_timed(n_steps, total_ms, phase_ms);
 }
 
 int64_t prismq_batch_atom_span(const prismq_batch* b) { return b ? b->atom_span : 0; }
@@ -1279,7 +1350,8 @@ prismq_status prismq_build_neighbors(prismq_system* sys, prismq_nlist_mode mode,
     return fail(PRISMQ_E_INVALID, "reference grid needs more than 32 cells per axis for this system");
   launch_control_cells(B->A, B->sys_span, kCtlForce, (int)mode, B->st);
   launch_nbr_build(B->A, B->atom_span, 0, B->st);
-  g_launches += 2;
+  launch_force(B->A, B->atom_span, false, B->st);  // also clears the rebuild queue
+  g_launches += 3;
   PQ_CK(cudaGetLastError());
   const int64_t n = R.n_atoms, ab = R.atom_b;
   std::vector<int> cnt(n);

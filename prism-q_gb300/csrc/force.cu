@@ -159,8 +159,26 @@ __device__ __forceinline__ double lane_sum(double v) {
 // its entries and accumulates them in int64; the lanes' int64 totals are then
 // summed exactly.  The decomposition depends only on the atom's own lists, so
 // an atom's force is identical whatever batch it is computed in.
-template <bool kEnergy>
-__global__ void __launch_bounds__(128) k_force(Arena A, int64_t n_span, int only_rebuilt) {
+// One ordinary pair, branch-free: force on i from j when r^2 lies in
+// [0.01, cutoff^2), an exact zero otherwise.
+__device__ __forceinline__ void pair_accumulate(const float4 pi, float qi, float2 li, const float4 pj, float2 lj,
+                                                float cut2, Acc& f) {
+  const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+  const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+  const bool in = r2 < cut2 && r2 >= kMinPairR2;
+  const float sig = li.x + lj.x, eps = li.y * lj.y, qq = qi * pj.w;
+  float inv_r, s6;
+  float fs = pair_scalar(fmaxf(r2, kMinPairR2), sig, eps, qq, inv_r, s6);
+  fs = in ? fs : 0.0f;
+  f.x -= fs * dx;
+  f.y -= fs * dy;
+  f.z -= fs * dz;
+}
+
+template <bool kEnergy, int kBlock, int kMinBlocks>
+__global__ void __launch_bounds__(kBlock, kMinBlocks) k_force(Arena A, int64_t n_span, int only_rebuilt) {
+  // the row builder that ran before this launch consumed the rebuild queue
+  if (blockIdx.x == 0 && threadIdx.x == 0) A.work_ctl[0] = 0;
   const int64_t a64 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 2;
   const int q = threadIdx.x & 3;
   bool live = a64 < n_span;
@@ -226,6 +244,36 @@ __global__ void __launch_bounds__(128) k_force(Arena A, int64_t n_span, int only
   float inv_rc = 0.f;
   if (kEnergy) inv_rc = rsqrtf(cut2);
   const int mine = n > q ? (n - q + kLanes - 1) / kLanes : 0;
+  if constexpr (!kEnergy) {
+    // Force-only path: entries are processed four at a time with every load
+    // issued before any arithmetic, and the cutoff is a select instead of a
+    // branch, so a lane keeps several gathers in flight and lanes never
+    // diverge.  Pairs outside the cutoff contribute an exact zero, so the sum
+    // is the same sequence of additions as a branching loop.
+    for (int t0 = 0; t0 < mine; t0 += 32) {
+      const int t1 = min(mine, t0 + 32);
+      int t = t0;
+      for (; t + 4 <= t1; t += 4) {
+        int j[4];
+        float4 pj[4];
+        float2 lj[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) j[u] = __ldg(row + (int64_t)(t + u) * 32);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          pj[u] = __ldg(pos + j[u]);
+          lj[u] = __ldg(A.lj + j[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) pair_accumulate(pi, qi, li, pj[u], lj[u], cut2, f);
+      }
+      for (; t < t1; ++t) {
+        const int j = __ldg(row + (int64_t)t * 32);
+        pair_accumulate(pi, qi, li, __ldg(pos + j), __ldg(A.lj + j), cut2, f);
+      }
+      f.flush();
+    }
+  } else
   for (int t0 = 0; t0 < mine; t0 += 32) {
     const int t1 = min(mine, t0 + 32);
 #pragma unroll 4
@@ -277,13 +325,38 @@ __global__ void __launch_bounds__(128) k_force(Arena A, int64_t n_span, int only
   }
 }
 
-void launch_force(const Arena& A, int64_t n_atoms_span, bool energy, cudaStream_t st, bool only_rebuilt) {
+// Launch shapes of the force-only kernel the autotuner chooses from: threads per
+// block and the minimum resident blocks per SM handed to the register allocator.
+// The shape changes neither the per-atom decomposition nor the results.
+struct ForceShape {
+  int block, min_blocks;
+};
+static const ForceShape kForceShapes[] = {{128, 1}, {128, 12}, {256, 6}, {64, 24}};
+
+int force_variant_count() { return (int)(sizeof(kForceShapes) / sizeof(kForceShapes[0])); }
+
+void force_variant_shape(int v, int* block, int* min_blocks) {
+  *block = kForceShapes[v].block;
+  *min_blocks = kForceShapes[v].min_blocks;
+}
+
+void launch_force(const Arena& A, int64_t n_atoms_span, bool energy, cudaStream_t st, bool only_rebuilt,
+                  int variant) {
   if (n_atoms_span <= 0) return;
-  const int64_t blocks = (n_atoms_span * kLanes + 127) / 128;
-  if (energy)
-    k_force<true><<<(unsigned)blocks, 128, 0, st>>>(A, n_atoms_span, only_rebuilt ? 1 : 0);
-  else
-    k_force<false><<<(unsigned)blocks, 128, 0, st>>>(A, n_atoms_span, only_rebuilt ? 1 : 0);
+  const int ob = only_rebuilt ? 1 : 0;
+  if (energy) {
+    const int64_t blocks = (n_atoms_span * kLanes + 127) / 128;
+    k_force<true, 128, 1><<<(unsigned)blocks, 128, 0, st>>>(A, n_atoms_span, ob);
+    return;
+  }
+  const int bs = kForceShapes[variant].block;
+  const unsigned blocks = (unsigned)((n_atoms_span * kLanes + bs - 1) / bs);
+  switch (variant) {
+    case 1: k_force<false, 128, 12><<<blocks, 128, 0, st>>>(A, n_atoms_span, ob); break;
+    case 2: k_force<false, 256, 6><<<blocks, 256, 0, st>>>(A, n_atoms_span, ob); break;
+    case 3: k_force<false, 64, 24><<<blocks, 64, 0, st>>>(A, n_atoms_span, ob); break;
+    default: k_force<false, 128, 1><<<blocks, 128, 0, st>>>(A, n_atoms_span, ob); break;
+  }
 }
 
 }  // namespace pq

@@ -13,12 +13,19 @@
 //                    cells and an ascending sort of each cell's contents, so
 //                    that rows come out in a deterministic order without a
 //                    per-row sort.
-//   k_nbr_build      one CTA per 32-atom group (one warp per atom): 27-cell
-//                    scan, exclusion window bitmask, ballot compaction into
-//                    shared-memory rows, then a cooperative coalesced write of
-//                    the rows in the interleaved layout the force kernel reads.
-// Complete mode uses cells at least as wide as the list radius (every pair
-// within r_list is found); REF27 mode reproduces the reference pair set.
+//                    The control kernel queues the 32-atom groups of every
+//                    rebuilding system on a device work list.
+//   k_nbr_build      persistent (one CTA per SM): pulls groups from the work
+//                    list; one warp per atom scans the stencil row by row (the
+//                    x-run of cells in one (y, z) row is one contiguous run of
+//                    sorted atoms, so warps stay full), applies the exclusion
+//                    window bitmask, ballot-compacts into shared-memory rows and
+//                    writes them cooperatively in the tiled layout the force
+//                    kernel reads.  Steps without rebuilds cost one empty pass.
+// Complete mode uses cells at least r_list/2 wide with a ±2 stencil (every
+// pair within r_list is found); REF27 mode reproduces the reference pair set.
+#include <algorithm>
+
 #include "pq_phases.cuh"
 
 namespace pq {
@@ -142,6 +149,7 @@ __global__ void __launch_bounds__(kCtlThreads) k_control_cells(Arena A, int mode
     Sp->steps_since_rebuild = rb ? 1 : Sp->steps_since_rebuild + 1;
     Sp->displaced = 0;
     Sp->rebuilding = rb ? 1 : 0;
+    if (rb) Sp->n_rebuilds += 1;
     if (nbr_override >= 0 && rb) Sp->nbr_mode = nbr_override;
     sh_rb = rb ? 1 : 0;
   }
@@ -321,121 +329,118 @@ __global__ void __launch_bounds__(kCtlThreads) k_control_cells(Arena A, int mode
     for (int k = lane; k < n; k += 32) A.cell_atoms[ab + b + k] = buf[k];
     __syncwarp();
   }
+  // queue this system's 32-atom groups for the row builder
+  __shared__ int sh_base;
+  const int ngroups = (na + 7) >> 3;  // 8-atom work items
   if (tid == 0) {
     Sp->built = 1;
+    sh_base = atomicAdd(&A.work_ctl[0], ngroups);
   }
+  __syncthreads();
+  for (int i = tid; i < ngroups; i += kCtlThreads) A.work[sh_base + i] = (ab >> 3) + i;
 }
 
-// One CTA per 32-atom group; warp w builds the row of atom 32*group + w.
-constexpr int kNbrThreads = 1024;
+// Persistent row builder: resident CTAs of eight warps pull 8-atom groups of
+// rebuilding systems from the work list; warp w builds the row of atom
+// 8*group + w and writes each kept neighbour straight into the tiled layout.
+constexpr int kNbrThreads = 256;
 
-__global__ void __launch_bounds__(kNbrThreads) k_nbr_build(Arena A, int64_t n_span, int exclude_exc) {
-  extern __shared__ int rows[];  // [32][kNbrCap]
-  __shared__ int cnt[32];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t g = blockIdx.x;
-  const int64_t a64 = g * 32 + warp;
+__device__ __forceinline__ void build_row(const Arena& A, int a, int exclude_exc, int lane, int* count_out) {
   int count = -1;
-  int* row = rows + warp * kNbrCap;
-  if (a64 < n_span) {
-    const int a = (int)a64;
-    const int s = A.atom_sys[a];
-    SysDev* Sp = s >= 0 ? &A.sys[s] : nullptr;
-    if (Sp && Sp->active && Sp->rebuilding && Sp->status == 0) {
-      const int ab = Sp->atom_begin;
-      const int mode = Sp->nbr_mode;
-      int dims[3];
-      float r2max;
-      if (mode == 1) {
-        dims[0] = Sp->ref_dims[0];
-        dims[1] = Sp->ref_dims[1];
-        dims[2] = Sp->ref_dims[2];
-      } else {
-        dims[0] = Sp->g_dims[0];
-        dims[1] = Sp->g_dims[1];
-        dims[2] = Sp->g_dims[2];
-      }
-      r2max = mode == 1 ? Sp->ref_r2 : Sp->rlist2;
-      const int* start = A.cell_start + Sp->cell_begin;
-      const float4 pi = A.pos[a];
-      const int cell = A.atom_cell[a];
-      const int cx = cell % dims[0], cy = (cell / dims[0]) % dims[1], cz = cell / (dims[0] * dims[1]);
-      const unsigned long long mask = exclude_exc ? A.mask_all[a] : A.mask_ref[a];
-      const int2 far = A.far[a];
-      count = 0;
-      bool overflow = false;
-      const int reach = mode == 1 ? 1 : 2;  // REF27: 27 cells of 10 Å; complete: 125 cells of >= r_list/2
-      for (int dz = -reach; dz <= reach; ++dz) {
-        const int z = cz + dz;
-        if (z < 0 || z >= dims[2]) continue;
-        for (int dy = -reach; dy <= reach; ++dy) {
-          const int y = cy + dy;
-          if (y < 0 || y >= dims[1]) continue;
-          for (int dx = -reach; dx <= reach; ++dx) {
-            const int x = cx + dx;
-            if (x < 0 || x >= dims[0]) continue;
-            const int c = x + y * dims[0] + z * dims[0] * dims[1];
-            const int b = start[c], e = start[c + 1];
-            for (int base = b; base < e; base += 32) {
-              const int k = base + lane;
-              int j = 0;
-              bool keep = false;
-              if (k < e) {
-                j = A.cell_atoms[ab + k];
-                if (j != a) {
-                  const float4 pj = A.pos[j];
-                  const float r2 = r2_nofma(pj.x - pi.x, pj.y - pi.y, pj.z - pi.z);
-                  keep = !(r2 > r2max);
-                  if (keep) {
-                    const int d = j - a;
-                    if (d >= -32 && d < 32) {
-                      if ((mask >> (d + 32)) & 1ull) keep = false;
-                    } else {
-                      for (int q = 0; q < far.y; ++q) {
-                        const int ent = A.far_list[far.x + q];
-                        if ((ent & 0x3fffffff) == j && (exclude_exc || !(ent & 0x40000000))) {
-                          keep = false;
-                          break;
-                        }
-                      }
+  const int s = A.atom_sys[a];
+  SysDev* Sp = s >= 0 ? &A.sys[s] : nullptr;
+  if (Sp && Sp->active && Sp->rebuilding && Sp->status == 0) {
+    const int ab = Sp->atom_begin;
+    const int mode = Sp->nbr_mode;
+    int dims[3];
+    if (mode == 1) {
+      dims[0] = Sp->ref_dims[0];
+      dims[1] = Sp->ref_dims[1];
+      dims[2] = Sp->ref_dims[2];
+    } else {
+      dims[0] = Sp->g_dims[0];
+      dims[1] = Sp->g_dims[1];
+      dims[2] = Sp->g_dims[2];
+    }
+    const float r2max = mode == 1 ? Sp->ref_r2 : Sp->rlist2;
+    const int* start = A.cell_start + Sp->cell_begin;
+    const float4 pi = A.pos[a];
+    const int cell = A.atom_cell[a];
+    const int cx = cell % dims[0], cy = (cell / dims[0]) % dims[1], cz = cell / (dims[0] * dims[1]);
+    const unsigned long long mask = exclude_exc ? A.mask_all[a] : A.mask_ref[a];
+    const int2 far = A.far[a];
+    const int reach = mode == 1 ? 1 : 2;  // REF27: 27 cells of 10 Å; complete: 125 cells of >= r_list/2
+    const int x0 = max(cx - reach, 0), x1 = min(cx + reach, dims[0] - 1);
+    count = 0;
+    bool overflow = false;
+    for (int dz = -reach; dz <= reach; ++dz) {
+      const int z = cz + dz;
+      if (z < 0 || z >= dims[2]) continue;
+      for (int dy = -reach; dy <= reach; ++dy) {
+        const int y = cy + dy;
+        if (y < 0 || y >= dims[1]) continue;
+        // the x-run of cells in one (y, z) row is one contiguous run of atoms
+        const int rowc = y * dims[0] + z * dims[0] * dims[1];
+        const int b = start[rowc + x0], e = start[rowc + x1 + 1];
+        for (int base = b; base < e; base += 32) {
+          const int k = base + lane;
+          int j = 0;
+          bool keep = false;
+          if (k < e) {
+            j = A.cell_atoms[ab + k];
+            if (j != a) {
+              const float4 pj = A.pos[j];
+              const float r2 = r2_nofma(pj.x - pi.x, pj.y - pi.y, pj.z - pi.z);
+              keep = !(r2 > r2max);
+              if (keep) {
+                const int d = j - a;
+                if (d >= -32 && d < 32) {
+                  if ((mask >> (d + 32)) & 1ull) keep = false;
+                } else {
+                  for (int q = 0; q < far.y; ++q) {
+                    const int ent = A.far_list[far.x + q];
+                    if ((ent & 0x3fffffff) == j && (exclude_exc || !(ent & 0x40000000))) {
+                      keep = false;
+                      break;
                     }
                   }
                 }
               }
-              const unsigned bal = __ballot_sync(0xffffffffu, keep);
-              const int add = __popc(bal);
-              if (count + add > kNbrCap) {
-                overflow = true;
-              } else {
-                if (keep) row[count + __popc(bal & ((1u << lane) - 1u))] = j;
-                count += add;
-              }
             }
+          }
+          const unsigned bal = __ballot_sync(0xffffffffu, keep);
+          const int add = __popc(bal);
+          if (count + add > kNbrCap) {
+            overflow = true;
+          } else {
+            if (keep) A.nbr[nbr_index(a, count + __popc(bal & ((1u << lane) - 1u)))] = j;
+            count += add;
           }
         }
       }
-      if (overflow) {
-        if (lane == 0) atomicOr(&Sp->status, kStNbrOverflow);
-        count = -1;
-      } else if (lane == 0) {
-        A.nnbr[a] = count;
-        A.xref[a] = pi;
-      }
+    }
+    if (overflow) {
+      if (lane == 0) atomicOr(&Sp->status, kStNbrOverflow);
+      count = -1;
+    } else if (lane == 0) {
+      A.nnbr[a] = count;
+      A.xref[a] = pi;
     }
   }
-  if (lane == 0) cnt[warp] = count;
-  __syncthreads();
-  // coalesced write of the tiled rows: the block's 32 atoms are four groups of
-  // eight; consecutive threads write consecutive words of nbr_index order
-  int maxc = 0;
-  for (int w = 0; w < 32; ++w) maxc = max(maxc, cnt[w]);
-  const int lines = (maxc + 3) >> 2;  // 4-entry lines per atom
-  int* out = A.nbr + g * 4 * (int64_t)kNbrCap * 8;
-  for (int idx = threadIdx.x; idx < 4 * lines * 32; idx += kNbrThreads) {
-    const int gi = idx / (lines * 32), rem = idx - gi * lines * 32;
-    const int t = rem >> 5, within = rem & 31;
-    const int w = gi * 8 + (within >> 2), k = 4 * t + (within & 3);
-    if (k < cnt[w]) out[(int64_t)gi * kNbrCap * 8 + t * 32 + within] = rows[w * kNbrCap + k];
+  *count_out = count;
+}
+
+// Warps walk the queued atoms round-robin (no shared counter, no atomics); the
+// force kernel that follows in the same stream clears the queue.
+__global__ void __launch_bounds__(kNbrThreads) k_nbr_build(Arena A, int64_t n_span, int exclude_exc) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = (int64_t)blockIdx.x * (kNbrThreads / 32) + (threadIdx.x >> 5);
+  const int64_t n_warps = (int64_t)gridDim.x * (kNbrThreads / 32);
+  const int64_t n_rows = (int64_t)A.work_ctl[0] * 8;
+  for (int64_t v = gw; v < n_rows; v += n_warps) {
+    const int64_t a64 = (int64_t)A.work[v >> 3] * 8 + (v & 7);
+    int count = -1;
+    if (a64 < n_span) build_row(A, (int)a64, exclude_exc, lane, &count);
   }
 }
 
@@ -452,14 +457,17 @@ void launch_control_cells(const Arena& A, int n_sys, int mode, int nbr_override,
 
 void launch_nbr_build(const Arena& A, int64_t n_atoms_span, int exclude_exceptions, cudaStream_t st) {
   if (n_atoms_span <= 0) return;
-  const size_t smem = (size_t)32 * kNbrCap * sizeof(int);
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_nbr_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    attr = true;
+  static int resident = 0;  // CTAs that fit on the GPU at once
+  if (!resident) {
+    int dev = 0, n_sm = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_nbr_build, kNbrThreads, 0);
+    resident = std::max(1, n_sm) * std::max(1, per_sm);
   }
-  const int64_t groups = (n_atoms_span + 31) / 32;
-  k_nbr_build<<<(unsigned)groups, kNbrThreads, smem, st>>>(A, n_atoms_span, exclude_exceptions);
+  const int64_t groups = (n_atoms_span + 7) / 8;
+  const int grid = (int)std::min<int64_t>(groups, resident);
+  k_nbr_build<<<grid, kNbrThreads, 0, st>>>(A, n_atoms_span, exclude_exceptions);
 }
 
 }  // namespace pq

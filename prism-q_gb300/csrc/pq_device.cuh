@@ -85,6 +85,7 @@ struct SysDev {
   int g_dims[3];
   int pad1;
   double vcom[3];
+  long long n_rebuilds;  // list builds so far (statistics)
 };
 
 // Per-atom incidence into bonded term arrays (reference: atom_bond_list etc.,
@@ -127,6 +128,9 @@ struct Arena {
   int* cell_start = nullptr;  // per system: cell_cap+1 entries
   int* cell_atoms = nullptr;  // per atom (sorted by cell)
   int* atom_cell = nullptr;
+  // work list of 32-atom groups to (re)build: [0] count, [1] fetch cursor, [2] CTAs done
+  int* work = nullptr;
+  int* work_ctl = nullptr;
   // systems
   SysDev* sys = nullptr;
 };
@@ -147,7 +151,9 @@ void launch_control_cells(const Arena& A, int n_sys, int mode, int nbr_mode_over
 void launch_nbr_build(const Arena& A, int64_t n_atoms_span, int exclude_exceptions,
                       cudaStream_t st);
 void launch_force(const Arena& A, int64_t n_atoms_span, bool energy, cudaStream_t st,
-                  bool only_rebuilt = false);
+                  bool only_rebuilt = false, int variant = 0);
+int force_variant_count();
+void force_variant_shape(int variant, int* block, int* min_blocks);
 void launch_integrate(const Arena& A, int64_t n_units_span, int mode, cudaStream_t st);
 void launch_debug_phases(const Arena& A, int64_t n_units_span, int set, long long step,
                          cudaStream_t st);

@@ -22,6 +22,10 @@
 
 namespace pq {
 
+// Loops over the (at most four) atoms of a unit are fully unrolled so the
+// unit's state stays in registers; the order of operations is unchanged.
+#define PQ_UNROLL _Pragma("unroll")
+
 struct UnitState {
   float x[4], y[4], z[4];
   float vx[4], vy[4], vz[4];
@@ -34,7 +38,8 @@ __device__ __forceinline__ void ou_half(UnitState& u, const SysDev& S, int atom_
                                         const int* atom_local, uint64_t step, uint32_t purpose) {
   if (S.gamma == 0.0f) return;
   const float c1 = S.c1;
-  for (int k = 0; k < u.n; ++k) {
+  PQ_UNROLL for (int k = 0; k < 4; ++k) {
+    if (k >= u.n) break;
     const float c2 = sqrtf((1.0f - c1 * c1) * kKcalToAmuA2Ps2 * kBoltzmann * S.temperature / u.m[k]);
     float z0, z1, z2;
     normal3(S.seed, S.stream, (uint32_t)atom_local[k], step, purpose, &z0, &z1, &z2);
@@ -46,7 +51,8 @@ __device__ __forceinline__ void ou_half(UnitState& u, const SysDev& S, int atom_
 }
 
 __device__ __forceinline__ void half_kick(UnitState& u, const SysDev& S) {
-  for (int k = 0; k < u.n; ++k) {
+  PQ_UNROLL for (int k = 0; k < 4; ++k) {
+    if (k >= u.n) break;
     const float kick = 0.5f * S.dt * kKcalToAmuA2Ps2 / u.m[k];
     if (S.gamma == 0.0f) {
       u.vx[k] += kick * u.fx[k];
@@ -71,7 +77,8 @@ __device__ __forceinline__ bool rattle(UnitState& u, const Unit& U, int max_iter
   const float ic = U.inv_mc, ih = U.inv_mh;
   for (int it = 0; it < max_iter; ++it) {
     float maxe = 0.0f;
-    for (int h = 1; h <= nh; ++h) {
+    PQ_UNROLL for (int h = 1; h <= 3; ++h) {
+      if (h > nh) break;
       const float rx = u.x[h] - u.x[0], ry = u.y[h] - u.y[0], rz = u.z[h] - u.z[0];
       const float r2 = rx * rx + ry * ry + rz * rz;
       if (!isfinite(r2) || r2 < 1.0e-12f) return false;
@@ -105,7 +112,8 @@ __device__ __forceinline__ bool shake(UnitState& u, const Unit& U, const float* 
   const float ic = U.inv_mc, ih = U.inv_mh;
   for (int it = 0; it < max_iter; ++it) {
     float maxe = 0.0f;
-    for (int h = 1; h <= nh; ++h) {
+    PQ_UNROLL for (int h = 1; h <= 3; ++h) {
+      if (h > nh) break;
       const float rx = u.x[h] - u.x[0], ry = u.y[h] - u.y[0], rz = u.z[h] - u.z[0];
       const float ox = sx[h] - sx[0], oy = sy[h] - sy[0], oz = sz[h] - sz[0];
       const float r2 = rx * rx + ry * ry + rz * rz;
@@ -143,7 +151,8 @@ __device__ __forceinline__ bool shake(UnitState& u, const Unit& U, const float* 
 }
 
 __device__ __forceinline__ void velocity_clamp(UnitState& u, const SysDev& S) {
-  for (int k = 0; k < u.n; ++k) {
+  PQ_UNROLL for (int k = 0; k < 4; ++k) {
+    if (k >= u.n) break;
     const float thermal = sqrtf(kKcalToAmuA2Ps2 * kBoltzmann * S.temperature / fmaxf(u.m[k], 1.0f));
     const float vmax = fmaxf(20.0f * thermal, 2.0f);
     const float mag = sqrtf(u.vx[k] * u.vx[k] + u.vy[k] * u.vy[k] + u.vz[k] * u.vz[k]);
@@ -158,7 +167,8 @@ __device__ __forceinline__ void velocity_clamp(UnitState& u, const SysDev& S) {
 __device__ __forceinline__ void load_unit(const Arena& A, const Unit& U, UnitState& u, int* local,
                                           int atom_begin) {
   u.n = U.nh < 0 ? 0 : 1 + U.nh;
-  for (int k = 0; k < u.n; ++k) {
+  PQ_UNROLL for (int k = 0; k < 4; ++k) {
+    if (k >= u.n) break;
     const int a = U.a[k];
     const float4 p = A.pos[a];
     const float4 v = A.vel[a];
@@ -177,7 +187,8 @@ __device__ __forceinline__ void load_unit(const Arena& A, const Unit& U, UnitSta
 }
 
 __device__ __forceinline__ void store_unit(const Arena& A, const Unit& U, const UnitState& u) {
-  for (int k = 0; k < u.n; ++k) {
+  PQ_UNROLL for (int k = 0; k < 4; ++k) {
+    if (k >= u.n) break;
     const int a = U.a[k];
     const float4 p = A.pos[a];
     A.pos[a] = make_float4(u.x[k], u.y[k], u.z[k], p.w);
@@ -206,7 +217,8 @@ __device__ __forceinline__ int phases_pre(UnitState& u, const Unit& U, const Sys
   half_kick(u, S);
   if (!rattle(u, U, S.max_iter)) return kStRattle;
   float sx[4], sy[4], sz[4];
-  for (int k = 0; k < u.n; ++k) {
+  PQ_UNROLL for (int k = 0; k < 4; ++k) {
+    if (k >= u.n) break;
     sx[k] = u.x[k];
     sy[k] = u.y[k];
     sz[k] = u.z[k];
@@ -219,7 +231,8 @@ __device__ __forceinline__ int phases_pre(UnitState& u, const Unit& U, const Sys
 }
 
 __device__ __forceinline__ bool unit_finite(const UnitState& u) {
-  for (int k = 0; k < u.n; ++k) {
+  PQ_UNROLL for (int k = 0; k < 4; ++k) {
+    if (k >= u.n) break;
     if (!isfinite(u.x[k]) || !isfinite(u.y[k]) || !isfinite(u.z[k]) || !isfinite(u.vx[k]) ||
         !isfinite(u.vy[k]) || !isfinite(u.vz[k]))
       return false;
@@ -232,7 +245,8 @@ __device__ __forceinline__ bool unit_finite(const UnitState& u) {
 __device__ __forceinline__ void check_displacement(const Arena& A, const Unit& U, const UnitState& u,
                                                    SysDev* S) {
   bool moved = false;
-  for (int k = 0; k < u.n; ++k) {
+  PQ_UNROLL for (int k = 0; k < 4; ++k) {
+    if (k >= u.n) break;
     const float4 r = A.xref[U.a[k]];
     const float dx = u.x[k] - r.x, dy = u.y[k] - r.y, dz = u.z[k] - r.z;
     if (dx * dx + dy * dy + dz * dz > S->half_skin2) moved = true;
