@@ -329,7 +329,7 @@ prismq_status lower_topology(const prismq_topology* T, Lowered* L) {
     L->ref_dims[d] = (int)std::min<long long>(v, kRefMaxDim);
     ref_cells *= L->ref_dims[d];
   }
-  L->cell_cap = (int)std::max<long long>({512LL, (long long)n / 4, L->ref_ok ? ref_cells : 0LL});
+  L->cell_cap = (int)std::max<long long>({1024LL, (long long)n / 2, L->ref_ok ? ref_cells : 0LL});
   return PRISMQ_OK;
 }
 
@@ -1050,7 +1050,7 @@ prismq_status prismq_batch_create(int64_t max_atoms, int32_t max_systems, prismq
   auto* B = new prismq_batch();
   const int64_t na = (max_atoms + 31) / 32 * 32 + 32 * (int64_t)max_systems;
   prismq_status rc = batch_alloc(B, na, max_systems, 2 * na, 4 * na, 8 * na, 48 * na, 8 * na, 2 * na,
-                                 2 * (na / 4 + 514 * (int64_t)max_systems));
+                                 2 * (na / 2 + 1026 * (int64_t)max_systems));
   if (rc != PRISMQ_OK) {
     delete B;
     return rc;

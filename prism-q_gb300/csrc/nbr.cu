@@ -200,12 +200,14 @@ __global__ void __launch_bounds__(kCtlThreads) k_control_cells(Arena A, int mode
       }
       // cells at least r_list/2·(1+1e-4) wide on every axis; the row builder
       // scans ±2 cells, which covers every pair within r_list
-      const float edge_min = sqrtf(Sp->rlist2) * 0.50005f;
+      // (y and z; x cells are only r_list/4 wide because rows are scanned as
+      // contiguous x-runs trimmed per atom to the sphere of radius r_list)
+      const float edge_yz = sqrtf(Sp->rlist2) * 0.50005f;
       int nd[3];
       float ext[3];
       for (int d = 0; d < 3; ++d) {
         ext[d] = fmaxf(gh[d] - gl[d], 1.0e-3f);
-        const float q = ext[d] / edge_min;
+        const float q = ext[d] / (d == 0 ? 0.5f * edge_yz : edge_yz);
         nd[d] = q >= 1.0f ? (int)q : 1;
         if (nd[d] > 1024) nd[d] = 1024;
       }
@@ -369,8 +371,15 @@ __device__ __forceinline__ void build_row(const Arena& A, int a, int exclude_exc
     const int cx = cell % dims[0], cy = (cell / dims[0]) % dims[1], cz = cell / (dims[0] * dims[1]);
     const unsigned long long mask = exclude_exc ? A.mask_all[a] : A.mask_ref[a];
     const int2 far = A.far[a];
-    const int reach = mode == 1 ? 1 : 2;  // REF27: 27 cells of 10 Å; complete: 125 cells of >= r_list/2
-    const int x0 = max(cx - reach, 0), x1 = min(cx + reach, dims[0] - 1);
+    // REF27: the reference's 27 cells of 10 Å.  Complete: rows of y/z cells
+    // (>= r_list/2 wide) within ±2, each scanned over the x-range that can hold
+    // atoms within r_list of atom a.  The trimming is conservative (cell
+    // indices are monotone in the coordinate, slab distances carry a 1e-3 Å
+    // margin), so it only removes candidates the r^2 test would reject.
+    const int reach = mode == 1 ? 1 : 2;
+    const float lox = Sp->g_lo[0], loy = Sp->g_lo[1], loz = Sp->g_lo[2];
+    const float ivx = Sp->g_inv_edge[0];
+    const float ey = 1.0f / Sp->g_inv_edge[1], ez = 1.0f / Sp->g_inv_edge[2];
     count = 0;
     bool overflow = false;
     for (int dz = -reach; dz <= reach; ++dz) {
@@ -379,6 +388,21 @@ __device__ __forceinline__ void build_row(const Arena& A, int a, int exclude_exc
       for (int dy = -reach; dy <= reach; ++dy) {
         const int y = cy + dy;
         if (y < 0 || y >= dims[1]) continue;
+        int x0, x1;
+        if (mode == 1) {
+          x0 = max(cx - 1, 0);
+          x1 = min(cx + 1, dims[0] - 1);
+        } else {
+          const float sy = fmaxf(0.0f, fmaxf((loy + (float)y * ey) - pi.y, pi.y - (loy + (float)(y + 1) * ey)));
+          const float sz = fmaxf(0.0f, fmaxf((loz + (float)z * ez) - pi.z, pi.z - (loz + (float)(z + 1) * ez)));
+          const float my = fmaxf(sy - 1.0e-3f, 0.0f), mz = fmaxf(sz - 1.0e-3f, 0.0f);
+          const float d2 = my * my + mz * mz;
+          if (d2 > r2max) continue;
+          const float xr = sqrtf(r2max - d2) + 1.0e-3f;
+          x0 = max((int)((pi.x - xr - lox) * ivx), 0);
+          x1 = min((int)((pi.x + xr - lox) * ivx), dims[0] - 1);
+          if (x0 > x1) continue;
+        }
         // the x-run of cells in one (y, z) row is one contiguous run of atoms
         const int rowc = y * dims[0] + z * dims[0] * dims[1];
         const int b = start[rowc + x0], e = start[rowc + x1 + 1];
