@@ -12,16 +12,16 @@
 //                    displacement), bounding box, counting sort of atoms into
 //                    cells and an ascending sort of each cell's contents, so
 //                    that rows come out in a deterministic order without a
-//                    per-row sort.
-//                    The control kernel queues the 32-atom groups of every
+//                    per-row sort.  It then queues the 8-atom groups of every
 //                    rebuilding system on a device work list.
-//   k_nbr_build      persistent (one CTA per SM): pulls groups from the work
-//                    list; one warp per atom scans the stencil row by row (the
-//                    x-run of cells in one (y, z) row is one contiguous run of
-//                    sorted atoms, so warps stay full), applies the exclusion
-//                    window bitmask, ballot-compacts into shared-memory rows and
-//                    writes them cooperatively in the tiled layout the force
-//                    kernel reads.  Steps without rebuilds cost one empty pass.
+//   k_nbr_build      persistent (all resident CTAs): warps walk the queued
+//                    atoms round-robin; one warp per atom scans the stencil row
+//                    by row (the x-run of cells in one (y, z) row is one
+//                    contiguous run of sorted atoms, trimmed per atom to the
+//                    sphere of radius r_list, so warps stay full), applies the
+//                    exclusion window bitmask and ballot-compacts the kept
+//                    atoms straight into the tiled layout the force kernel
+//                    reads.  Steps without rebuilds cost one empty pass.
 // Complete mode uses cells at least r_list/2 wide with a ±2 stencil (every
 // pair within r_list is found); REF27 mode reproduces the reference pair set.
 #include <algorithm>
@@ -331,7 +331,7 @@ __global__ void __launch_bounds__(kCtlThreads) k_control_cells(Arena A, int mode
     for (int k = lane; k < n; k += 32) A.cell_atoms[ab + b + k] = buf[k];
     __syncwarp();
   }
-  // queue this system's 32-atom groups for the row builder
+  // queue this system's 8-atom groups for the row builder
   __shared__ int sh_base;
   const int ngroups = (na + 7) >> 3;  // 8-atom work items
   if (tid == 0) {

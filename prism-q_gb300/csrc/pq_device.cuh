@@ -128,7 +128,7 @@ struct Arena {
   int* cell_start = nullptr;  // per system: cell_cap+1 entries
   int* cell_atoms = nullptr;  // per atom (sorted by cell)
   int* atom_cell = nullptr;
-  // work list of 32-atom groups to (re)build: [0] count, [1] fetch cursor, [2] CTAs done
+  // work list of 8-atom groups to (re)build; work_ctl[0] = queued groups
   int* work = nullptr;
   int* work_ctl = nullptr;
   // systems
