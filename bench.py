@@ -49,7 +49,7 @@ def args_parse():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="batch256", choices=["batch256", "plain2500", "large100k"])
+    ap.add_argument("--workload", default="batch256", choices=["batch256", "plain2500", "large100k", "serve"])
     ap.add_argument("--systems", type=int, default=256)
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -57,6 +57,11 @@ def args_parse():
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--equil", type=int, default=400,
                     help="MD steps run on the freshly grown systems before warm-up (equilibration)")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving leg of the default run")
+    ap.add_argument("--serve-jobs", type=int, default=200)
+    ap.add_argument("--serve-rate", type=float, default=50.0, help="Poisson arrival rate, jobs/s")
+    ap.add_argument("--serve-hbm-gb", type=float, default=16.0, help="device bytes of the server arena")
+    ap.add_argument("--serve-pool", type=int, default=24, help="distinct seeded topologies the jobs draw from")
     return ap.parse_args()
 
 
@@ -237,6 +242,71 @@ def cpu_reference_rate(pq, topos, steps_cap: int, seconds: float, threads: int) 
     return atoms_steps / wall, ", ".join(desc)
 
 
+# ------------------------------------------------------------------ serving
+def run_serving(args, pq) -> dict:
+    """Poisson stream of MD jobs through the job server (prismq_server_*).
+
+    Jobs: atoms log-uniform in [300, 20000] (chains of 30-2000 residues drawn
+    from a pool of seeded topologies at stratified sizes), steps uniform in
+    [500, 5000], arrivals Poisson at --serve-rate.  Every job has its own noise
+    stream.  Latency = submit -> final state written to the job's host buffers.
+    """
+    rng = np.random.default_rng(args.seed + 4)
+    P = args.serve_pool
+    lo, hi = math.log(30), math.log(2000)
+    residues = [int(round(math.exp(lo + (i + 0.5) / P * (hi - lo)))) for i in range(P)]
+    specs = [(1, r, 0.0) for r in residues]
+    pool = build_topologies(pq, specs, list(range(P)), args.seed + 17)
+    n = args.serve_jobs
+    pick = rng.integers(0, P, size=n)
+    steps = rng.integers(500, 5001, size=n)
+    arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, size=n))
+    srv = pq.Server(int(args.serve_hbm_gb * 2**30), max_systems=1024, chunk_steps=50)
+    # warm-up: first admissions tune the force kernel and capture the graph
+    for k in range(4):
+        srv.submit(pool[k * (P // 4)], 100, pq.Params(stream=900000 + k), want_state=False)
+    got = 0
+    while got < 4:
+        got += len(srv.poll(wait_ms=500))
+    base = srv.stats()
+    results = []
+    t0 = time.perf_counter()
+    for k in range(n):
+        while True:
+            wait = arrivals[k] - (time.perf_counter() - t0)
+            if wait <= 0:
+                break
+            results += srv.poll(wait_ms=max(1, int(wait * 1000)))
+        srv.submit(pool[pick[k]], int(steps[k]), pq.Params(stream=k), tag=k)
+    t_end = time.time() + 600
+    while len(results) < n and time.time() < t_end:
+        results += srv.poll(wait_ms=200)
+    st = srv.stats()
+    srv.close()
+    ok = [r for r in results if r.ok]
+    lat = np.array([r.latency_s for r in ok])
+    wait = np.array([r.start_s - r.submit_s for r in ok])
+    first = min(r.submit_s for r in results)
+    last = max(r.end_s for r in results)
+    atom_steps = float(sum(r.n_atoms * r.steps_done for r in ok))
+    atoms = np.array([pool[i].n_atoms for i in pick])
+    return {
+        "value": atom_steps / (last - first), "unit": "atom-steps/s",
+        "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                      "mean": float(lat.mean()), "max": float(lat.max())},
+        "queue_wait_s": {"p50": float(np.percentile(wait, 50)), "p99": float(np.percentile(wait, 99))},
+        "jobs": n, "completed": len(ok), "failed": len(results) - len(ok),
+        "arrival_rate_per_s": args.serve_rate, "span_s": last - first,
+        "job_atoms": {"mean": float(atoms.mean()), "min": int(atoms.min()), "max": int(atoms.max())},
+        "job_steps_mean": float(steps.mean()),
+        "offered_atom_steps_per_s": float((atoms * steps).sum() / arrivals[-1]),
+        "gpu_busy_frac": (st["busy_s"] - base["busy_s"]) / max(last - first, 1e-9),
+        "chunks": st["chunks"] - base["chunks"], "arena_atoms": st["capacity_atoms"],
+        "arena_bytes": st["device_bytes"],
+        "sample": f"{n} jobs from a pool of {P} seeded chains (30-2000 residues), Poisson arrivals",
+    }
+
+
 # ------------------------------------------------------------------ main legs
 def run_reference(args, pq, rank, world):
     if rank != 0:
@@ -388,9 +458,11 @@ def run_ours(args, pq, rank, world):
         "roofline": roof, "hbm": hbm, "kernel_avg_ms": phase_avg, "gpu_launches": int(launches), "clocks": clk,
         "cpu_baseline": cpu,
     }
+    batch.close()
+    if rank == 0 and world == 1 and args.workload == "batch256" and not args.no_serve:
+        line["serving"] = run_serving(args, pq)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    batch.close()
 
 
 def main():
@@ -402,6 +474,23 @@ def main():
     rank, world, _ = dist_setup(args.gpus)
     if args.impl == "reference":
         run_reference(args, pq, rank, world)
+    elif args.workload == "serve":
+        if rank == 0:
+            launches0 = pq.kernel_launches()
+            clocks = ClockSampler()
+            clocks.start()
+            sv = run_serving(args, pq)
+            clk = clocks.stop()
+            line = {"metric": METRIC, "value": sv["value"], "unit": "atom-steps/s", "n_gpus": 1,
+                    "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+                    "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded poly-alanine jobs; no dataset)",
+                    "config": {"workload": "serve", "jobs": sv["jobs"], "arrival_rate_per_s": sv["arrival_rate_per_s"],
+                               "parallelism": "one job server on 1 GPU"},
+                    "e2e": {"value": sv["value"], "unit": "atom-steps/s",
+                            "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,
+                            "note": "served throughput is end to end: topologies in, final states out"},
+                    "serving": sv, "gpu_launches": int(pq.kernel_launches() - launches0), "clocks": clk}
+            print(json.dumps(line), flush=True)
     else:
         run_ours(args, pq, rank, world)
     if world > 1:

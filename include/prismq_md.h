@@ -259,6 +259,81 @@ prismq_status prismq_batch_get_state_all(prismq_batch* b, float* xyz, float* vxy
 prismq_status prismq_batch_run_timed(prismq_batch* b, int64_t n_steps, float* total_ms, float* phase_ms);
 int32_t prismq_batch_resident_systems(const prismq_batch* b);
 
+/* ---- job server: continuous batching of independent MD jobs ----
+ *
+ * The reference has no batched or served form of this path (its parallel
+ * replica entry points bail out, fused_engine.rs:18306 and :18433); a caller
+ * runs one NhsAmberFusedEngine per system (new_on_stream :10800, run :23911,
+ * get_positions :24117).  The server replaces that loop: one worker thread owns
+ * a batch arena sized from max_hbm_bytes, admits queued jobs whenever their
+ * atoms and terms fit in the free arena ranges (admission by HBM footprint),
+ * advances every resident job together in chunks of at most chunk_steps steps
+ * (each chunk ends exactly where the nearest job finishes), and retires
+ * finished jobs between chunks.  A job's trajectory depends only on its own
+ * topology and params, never on which other jobs share the GPU: results are
+ * bit-identical to running the job alone.
+ *
+ * Threading: every prismq_server_* call is internally locked and may come
+ * from any thread. */
+
+typedef struct prismq_server prismq_server;
+
+typedef struct prismq_server_config {
+  int32_t max_systems;  /* resident jobs at most (<= 0 selects 1024) */
+  int32_t chunk_steps;  /* steps between scheduling points (<= 0 selects 50) */
+  double max_bypass_s;  /* how long later jobs may overtake a queued job that does
+                           not fit yet (< 0 selects 1.0; 0 = strict FIFO) */
+} prismq_server_config;
+
+typedef struct prismq_job {
+  const prismq_topology* topology; /* validated and copied by submit */
+  prismq_params params;            /* seed/stream select the job's noise */
+  int64_t n_steps;                 /* >= 1 */
+  float* positions_out;            /* host float[3N] or NULL: final positions */
+  float* velocities_out;           /* host float[3N] or NULL: final velocities */
+  uint64_t tag;                    /* echoed in the result */
+} prismq_job;
+
+typedef struct prismq_job_result {
+  int64_t job_id;
+  uint64_t tag;
+  prismq_status status;  /* PRISMQ_OK, or why the job stopped */
+  int32_t n_atoms;
+  int64_t steps_done;
+  double submit_s;  /* server clock (seconds since create) at submit */
+  double start_s;   /* admission into the arena */
+  double end_s;     /* results written to the job's buffers */
+  char message[160];
+} prismq_job_result;
+
+typedef struct prismq_server_stats {
+  int64_t submitted, completed, failed, queued, resident_jobs, resident_atoms;
+  int64_t capacity_atoms;  /* arena atom capacity */
+  int64_t device_bytes;    /* device memory held by the arena */
+  int64_t chunks;          /* batch step calls so far */
+  double atom_steps;       /* atom-steps completed by all jobs */
+  double busy_s;           /* worker time inside batch steps */
+  double uptime_s;
+} prismq_server_stats;
+
+void prismq_server_config_default(prismq_server_config* cfg);
+/* Reserve an arena of at most max_hbm_bytes device bytes and start the
+ * worker.  cfg may be NULL (defaults). */
+prismq_status prismq_server_create(int64_t max_hbm_bytes, const prismq_server_config* cfg,
+                                   prismq_server** out);
+/* Validate and queue a job; *job_id receives its id.  PRISMQ_E_CAPACITY if the
+ * job could never fit in the arena.  The job's output buffers must stay valid
+ * until its result has been polled. */
+prismq_status prismq_server_submit(prismq_server* s, const prismq_job* job, int64_t* job_id);
+/* Move up to cap finished results into out (completion order); waits up to
+ * wait_ms for at least one when none is ready.  *n receives the count. */
+prismq_status prismq_server_poll(prismq_server* s, prismq_job_result* out, int32_t cap, int32_t* n,
+                                 int32_t wait_ms);
+prismq_status prismq_server_stats_get(prismq_server* s, prismq_server_stats* out);
+/* Stop the worker after its current chunk; queued and resident jobs are
+ * dropped without results. */
+void prismq_server_destroy(prismq_server* s);
+
 /* ---- neighbour rows without device allocation ----
  *
  * No counterpart in the reference: it serves callers that cannot allocate

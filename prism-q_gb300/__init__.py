@@ -82,6 +82,27 @@ class ParamsStruct(ctypes.Structure):
                 ("seed", ctypes.c_uint32), ("stream", ctypes.c_uint32)]
 
 
+class ServerConfigStruct(ctypes.Structure):
+    _fields_ = [("max_systems", ctypes.c_int32), ("chunk_steps", ctypes.c_int32), ("max_bypass_s", ctypes.c_double)]
+
+
+class JobStruct(ctypes.Structure):
+    _fields_ = [("topology", _P), ("params", ParamsStruct), ("n_steps", ctypes.c_int64),
+                ("positions_out", _P), ("velocities_out", _P), ("tag", ctypes.c_uint64)]
+
+
+class JobResultStruct(ctypes.Structure):
+    _fields_ = [("job_id", ctypes.c_int64), ("tag", ctypes.c_uint64), ("status", ctypes.c_int),
+                ("n_atoms", ctypes.c_int32), ("steps_done", ctypes.c_int64), ("submit_s", ctypes.c_double),
+                ("start_s", ctypes.c_double), ("end_s", ctypes.c_double), ("message", ctypes.c_char * 160)]
+
+
+class ServerStatsStruct(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int64) for n in ("submitted", "completed", "failed", "queued", "resident_jobs",
+                                                  "resident_atoms", "capacity_atoms", "device_bytes", "chunks")] + \
+               [(n, ctypes.c_double) for n in ("atom_steps", "busy_s", "uptime_s")]
+
+
 # numpy dtypes with the same layout as the C structs
 BOND_DT = np.dtype([("i", "<i4"), ("j", "<i4"), ("r0", "<f4"), ("k", "<f4")])
 ANGLE_DT = np.dtype([("i", "<i4"), ("j", "<i4"), ("k", "<i4"), ("theta0", "<f4"), ("force_k", "<f4")])
@@ -151,6 +172,12 @@ def load() -> ctypes.CDLL:
         "prismq_batch_run_timed": (I, [P, i64, P, P]),
         "prismq_batch_counters": (I, [P, ctypes.c_int32, P]),
         "prismq_batch_tuning": (I, [P, P]),
+        "prismq_server_config_default": (None, [P]),
+        "prismq_server_create": (I, [i64, P, P]),
+        "prismq_server_submit": (I, [P, P, P]),
+        "prismq_server_poll": (I, [P, P, ctypes.c_int32, P, ctypes.c_int32]),
+        "prismq_server_stats_get": (I, [P, P]),
+        "prismq_server_destroy": (None, [P]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(L, name)
@@ -473,3 +500,87 @@ class Batch:
     @property
     def resident_systems(self) -> int:
         return int(load().prismq_batch_resident_systems(self.h))
+
+
+# ---------------------------------------------------------------- job server
+@dataclass
+class JobResult:
+    job_id: int
+    tag: int
+    status: int
+    n_atoms: int
+    steps_done: int
+    submit_s: float
+    start_s: float
+    end_s: float
+    message: str
+    positions: np.ndarray | None
+    velocities: np.ndarray | None
+
+    @property
+    def latency_s(self) -> float:
+        return self.end_s - self.submit_s
+
+    @property
+    def ok(self) -> bool:
+        return self.status == 0
+
+
+class Server:
+    """Continuous-batching MD job server (prismq_server_*): one worker thread
+    owns a device arena of at most max_hbm_bytes, admits queued jobs as arena
+    space frees up and advances every resident job together."""
+
+    def __init__(self, max_hbm_bytes: int, max_systems: int = 1024, chunk_steps: int = 50,
+                 max_bypass_s: float = 1.0):
+        cfg = ServerConfigStruct(max_systems, chunk_steps, max_bypass_s)
+        self.h = ctypes.c_void_p()
+        _check(load().prismq_server_create(int(max_hbm_bytes), ctypes.byref(cfg), ctypes.byref(self.h)))
+        self._out: dict[int, tuple] = {}
+
+    def close(self) -> None:
+        if self.h:
+            load().prismq_server_destroy(self.h)
+            self.h = None
+            self._out.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def submit(self, topology: Topology, n_steps: int, params: Params | None = None, tag: int = 0,
+               want_state: bool = True) -> int:
+        n = topology.n_atoms
+        x = np.zeros((n, 3), np.float32) if want_state else None
+        v = np.zeros((n, 3), np.float32) if want_state else None
+        t = topology.struct()
+        job = JobStruct(ctypes.cast(ctypes.pointer(t), _P), (params or Params()).struct(), int(n_steps),
+                        _ptr(x), _ptr(v), int(tag) & 0xffffffffffffffff)
+        jid = ctypes.c_int64()
+        _check(load().prismq_server_submit(self.h, ctypes.byref(job), ctypes.byref(jid)))
+        self._out[jid.value] = (x, v)  # the worker writes here when the job ends
+        return jid.value
+
+    def poll(self, wait_ms: int = 0, max_results: int = 256) -> list[JobResult]:
+        buf = (JobResultStruct * max_results)()
+        n = ctypes.c_int32()
+        _check(load().prismq_server_poll(self.h, buf, max_results, ctypes.byref(n), int(wait_ms)))
+        out = []
+        for r in buf[:n.value]:
+            x, v = self._out.pop(r.job_id, (None, None))
+            out.append(JobResult(r.job_id, r.tag, r.status, r.n_atoms, r.steps_done, r.submit_s, r.start_s,
+                                 r.end_s, r.message.decode(errors="replace"), x, v))
+        return out
+
+    def stats(self) -> dict:
+        st = ServerStatsStruct()
+        _check(load().prismq_server_stats_get(self.h, ctypes.byref(st)))
+        return {name: getattr(st, name) for name, _ in st._fields_}

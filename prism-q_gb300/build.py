@@ -32,6 +32,7 @@ UNITS = {
     "nbr.cu": ["--fmad=false"],
     "noalloc.cu": ["--fmad=false"],
     "topology.cpp": [],
+    "server.cpp": [],
 }
 
 

@@ -520,7 +520,9 @@ struct prismq_batch {
   // (three launches each, CUDA events) and keep the fastest.  The shapes give
   // identical forces, so the choice affects speed only.
   prismq_status tune_force() {
-    if (force_variant >= 0 && tuned_span == atom_span) return PRISMQ_OK;
+    // re-tune only when the resident span has changed by 2x or more since the
+    // last tuning, so that admission churn in a server does not re-time shapes
+    if (force_variant >= 0 && atom_span <= 2 * tuned_span && 2 * atom_span >= tuned_span) return PRISMQ_OK;
     cudaEvent_t e0, e1;
     PQ_CK(cudaEventCreate(&e0));
     PQ_CK(cudaEventCreate(&e1));
@@ -687,14 +689,17 @@ struct prismq_system {
 
 namespace {
 
+// Allocate the arena.  With `dry` set nothing touches the device: *bytes_out
+// receives the device bytes the same call would allocate.
 prismq_status batch_alloc(prismq_batch* B, int64_t atom_cap, int sys_cap, int64_t bond_cap,
                           int64_t angle_cap, int64_t dih_cap, int64_t inc_cap, int64_t ex_cap,
-                          int64_t far_cap, int64_t cell_cap) {
+                          int64_t far_cap, int64_t cell_cap, bool dry = false, int64_t* bytes_out = nullptr) {
   int ndev = 0;
-  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+  if (!dry && (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)) {
     cudaGetLastError();
     return fail(PRISMQ_E_NO_DEVICE, "no CUDA device visible");
   }
+  int64_t total = 0;
   atom_cap = (atom_cap + 31) / 32 * 32;
   Arena& A = B->A;
   A.atom_cap = atom_cap;
@@ -707,8 +712,13 @@ prismq_status batch_alloc(prismq_batch* B, int64_t atom_cap, int sys_cap, int64_
   A.far_cap = std::max<int64_t>(far_cap, 1);
   A.cell_cap = std::max<int64_t>(cell_cap, 1);
   A.sys_cap = sys_cap;
-  PQ_CK(cudaStreamCreateWithFlags(&B->st, cudaStreamNonBlocking));
-#define PQ_ALLOC(ptr, count) PQ_CK(cudaMalloc((void**)&(ptr), sizeof(*(ptr)) * (size_t)(count)))
+  if (!dry) PQ_CK(cudaStreamCreateWithFlags(&B->st, cudaStreamNonBlocking));
+#define PQ_ALLOC(ptr, count)                                  \
+  do {                                                        \
+    const size_t nb_ = sizeof(*(ptr)) * (size_t)(count);      \
+    total += (int64_t)nb_;                                    \
+    if (!dry) PQ_CK(cudaMalloc((void**)&(ptr), nb_));         \
+  } while (0)
   PQ_ALLOC(A.pos, atom_cap);
   PQ_ALLOC(A.vel, atom_cap);
   PQ_ALLOC(A.lj, atom_cap);
@@ -741,6 +751,8 @@ prismq_status batch_alloc(prismq_batch* B, int64_t atom_cap, int sys_cap, int64_
   PQ_ALLOC(B->d_stage, 3 * atom_cap);
   PQ_ALLOC(B->d_stage2, 3 * atom_cap);
 #undef PQ_ALLOC
+  if (bytes_out) *bytes_out = total;
+  if (dry) return PRISMQ_OK;
   PQ_CK(cudaMemsetAsync(A.sys, 0, sizeof(SysDev) * sys_cap, B->st));
   PQ_CK(cudaMemsetAsync(A.nnbr, 0, sizeof(int) * atom_cap, B->st));
   PQ_CK(cudaMemsetAsync(A.work_ctl, 0, sizeof(int) * 4, B->st));
@@ -762,6 +774,17 @@ prismq_status batch_alloc(prismq_batch* B, int64_t atom_cap, int sys_cap, int64_
   B->slots.resize(sys_cap);
   B->h_sys.resize(sys_cap);
   return PRISMQ_OK;
+}
+
+// Arena capacities of a batch for max_atoms atoms in max_systems systems:
+// per-atom term capacities cover poly-peptide topologies with margin (bonds
+// 2/atom, angles 4, torsion terms 8, incidence entries 48, exceptions 8, far
+// exclusions 2) and every system may pad its atom range to 32.
+prismq_status batch_alloc_sized(prismq_batch* B, int64_t max_atoms, int32_t max_systems, bool dry,
+                                int64_t* bytes_out) {
+  const int64_t na = (max_atoms + 31) / 32 * 32 + 32 * (int64_t)max_systems;
+  return batch_alloc(B, na, max_systems, 2 * na, 4 * na, 8 * na, 48 * na, 8 * na, 2 * na,
+                     2 * (na / 2 + 1026 * (int64_t)max_systems), dry, bytes_out);
 }
 
 template <class T>
@@ -1048,9 +1071,7 @@ void prismq_topology_free(prismq_topology_buf* buf) { delete buf; }
 prismq_status prismq_batch_create(int64_t max_atoms, int32_t max_systems, prismq_batch** out) {
   if (!out || max_atoms <= 0 || max_systems <= 0) return fail(PRISMQ_E_INVALID, "invalid batch size");
   auto* B = new prismq_batch();
-  const int64_t na = (max_atoms + 31) / 32 * 32 + 32 * (int64_t)max_systems;
-  prismq_status rc = batch_alloc(B, na, max_systems, 2 * na, 4 * na, 8 * na, 48 * na, 8 * na, 2 * na,
-                                 2 * (na / 2 + 1026 * (int64_t)max_systems));
+  prismq_status rc = batch_alloc_sized(B, max_atoms, max_systems, false, nullptr);
   if (rc != PRISMQ_OK) {
     delete B;
     return rc;
@@ -1403,3 +1424,80 @@ prismq_status prismq_debug_phases(prismq_system* sys, prismq_phase_set set, int6
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Hooks for the job server (server.cpp): a job is lowered on the submitting
+// thread and admitted, already lowered, by the server's worker thread.
+// ===========================================================================
+namespace pq {
+
+struct PreparedSystem {
+  Lowered L;
+  prismq_params p;
+};
+
+prismq_status prepare_system(const prismq_topology* t, const prismq_params* p, PreparedSystem** out) {
+  if (!out) return fail(PRISMQ_E_INVALID, "NULL argument");
+  *out = nullptr;
+  prismq_status rc = check_params(p);
+  if (rc != PRISMQ_OK) return rc;
+  auto* S = new PreparedSystem();
+  rc = lower_topology(t, &S->L);
+  if (rc != PRISMQ_OK) {
+    delete S;
+    return rc;
+  }
+  init_velocities(&S->L, *p);
+  S->p = *p;
+  *out = S;
+  return PRISMQ_OK;
+}
+
+void free_prepared(PreparedSystem* s) { delete s; }
+
+int32_t prepared_atoms(const PreparedSystem* s) { return s ? s->L.n : 0; }
+
+prismq_status admit_prepared(prismq_batch* b, const PreparedSystem* s, int32_t* slot) {
+  if (!b || !s || !slot) return fail(PRISMQ_E_INVALID, "NULL argument");
+  int sl = -1;
+  prismq_status rc = batch_admit(b, s->L, s->p, &sl);
+  if (rc != PRISMQ_OK) return rc;
+  *slot = sl;
+  return PRISMQ_OK;
+}
+
+// The largest batch (in atoms, a multiple of 32) whose arena fits in
+// max_bytes of device memory.
+prismq_status batch_create_for_bytes(int64_t max_bytes, int32_t max_systems, prismq_batch** out,
+                                     int64_t* atom_cap, int64_t* device_bytes) {
+  if (!out || max_bytes <= 0 || max_systems <= 0) return fail(PRISMQ_E_INVALID, "invalid server size");
+  int64_t b0 = 0, b1 = 0;
+  {
+    prismq_batch probe;
+    batch_alloc_sized(&probe, 32, max_systems, true, &b0);
+    batch_alloc_sized(&probe, 32 + 32 * 1024, max_systems, true, &b1);
+  }
+  const int64_t per32 = std::max<int64_t>((b1 - b0) / 1024, 1);  // bytes per 32 atoms
+  int64_t n = max_bytes > b0 ? 32 + (max_bytes - b0) / per32 * 32 : 0;
+  for (; n >= 32; n -= 32) {
+    prismq_batch probe;
+    int64_t bytes = 0;
+    batch_alloc_sized(&probe, n, max_systems, true, &bytes);
+    if (bytes <= max_bytes) break;
+  }
+  if (n < 32)
+    return fail(PRISMQ_E_CAPACITY, "max_hbm_bytes holds no arena for " + std::to_string(max_systems) + " systems");
+  auto* B = new prismq_batch();
+  int64_t bytes = 0;
+  prismq_status rc = batch_alloc_sized(B, n, max_systems, false, &bytes);
+  if (rc != PRISMQ_OK) {
+    delete B;
+    return rc;
+  }
+  *out = B;
+  if (atom_cap) *atom_cap = n;
+  if (device_bytes) *device_bytes = bytes;
+  return PRISMQ_OK;
+}
+
+}  // namespace pq

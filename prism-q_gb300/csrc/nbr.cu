@@ -146,8 +146,13 @@ __global__ void __launch_bounds__(kCtlThreads) k_control_cells(Arena A, int mode
       Sp->step = Sp->step + 1;
     }
     if (atomicAdd(&Sp->status, 0) != 0) rb = false;
-    Sp->steps_since_rebuild = rb ? 1 : Sp->steps_since_rebuild + 1;
-    Sp->displaced = 0;
+    // A prime pass (another system was admitted or reset) leaves the schedule
+    // of the systems it does not rebuild untouched, so a system's trajectory
+    // never depends on what else shares the batch.
+    if (mode != kCtlPrime || rb) {
+      Sp->steps_since_rebuild = rb ? 1 : Sp->steps_since_rebuild + 1;
+      Sp->displaced = 0;
+    }
     Sp->rebuilding = rb ? 1 : 0;
     if (rb) Sp->n_rebuilds += 1;
     if (nbr_override >= 0 && rb) Sp->nbr_mode = nbr_override;

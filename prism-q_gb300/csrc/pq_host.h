@@ -47,6 +47,19 @@ struct HostTopology {
 bool polyala_build(int n_chains, int n_res, uint64_t seed, double density, double box_edge,
                    HostTopology* T, std::string* err);
 
+// Engine hooks for the job server (defined in engine.cu).  A job's topology is
+// validated and lowered once on the submitting thread (prepare_system); the
+// worker admits the lowered form into its batch (admit_prepared).  Errors are
+// reported through prismq_last_error() of the calling thread.
+void set_last_error(const std::string& msg);  // the message prismq_last_error() returns on this thread
+struct PreparedSystem;
+prismq_status prepare_system(const prismq_topology* t, const prismq_params* p, PreparedSystem** out);
+void free_prepared(PreparedSystem* s);
+int32_t prepared_atoms(const PreparedSystem* s);
+prismq_status admit_prepared(prismq_batch* b, const PreparedSystem* s, int32_t* slot);
+prismq_status batch_create_for_bytes(int64_t max_bytes, int32_t max_systems, prismq_batch** out,
+                                     int64_t* atom_cap, int64_t* device_bytes);
+
 }  // namespace pq
 
 struct prismq_topology_buf {

@@ -1,0 +1,160 @@
+"""Continuous batching and the job server.
+
+The property under test is the serving contract: a job's result is the same,
+bit for bit, whether it runs alone or shares the GPU with jobs that arrive,
+finish and fail around it.  The reference has no batched form of this path
+(fused_engine.rs:18306, :18433 bail out), so "alone" is one system in its own
+batch, stepped in one call.
+"""
+from __future__ import annotations
+
+import ctypes
+import time
+
+import numpy as np
+import pytest
+
+
+def _alone(pq, topo, params, n_steps):
+    b = pq.Batch(max_atoms=topo.n_atoms + 64, max_systems=1)
+    s = b.add_system(topo, params)
+    b.step(n_steps)
+    x, v = b.get_state(s)
+    b.close()
+    return x, v
+
+
+def _drain(server, n, timeout_s=240.0):
+    out = []
+    t_end = time.time() + timeout_s
+    while len(out) < n and time.time() < t_end:
+        out += server.poll(wait_ms=200)
+    assert len(out) == n, f"only {len(out)} of {n} results arrived"
+    return {r.job_id: r for r in out}
+
+
+# ---------------------------------------------------------------- CPU checks
+def test_server_structs_match_the_header(pq):
+    # sizes of the C structs on LP64 (x86-64 and aarch64): the ctypes mirrors
+    # must agree or every field after the first mismatch is misread
+    assert ctypes.sizeof(pq.ServerConfigStruct) == 16
+    assert ctypes.sizeof(pq.JobStruct) == 80
+    assert ctypes.sizeof(pq.JobResultStruct) == 216
+    assert ctypes.sizeof(pq.ServerStatsStruct) == 96
+
+
+def test_server_without_device_fails_loudly(pq):
+    if pq.device_count() > 0:
+        pytest.skip("a GPU is visible")
+    with pytest.raises(pq.PrismQError) as e:
+        pq.Server(1 << 30)
+    assert e.value.status == 3  # E_NO_DEVICE
+
+
+# ---------------------------------------------------------------- GPU
+@pytest.fixture(scope="module")
+def mix(pq):
+    """Three chains of different sizes with their own noise streams."""
+    return [(pq.Topology.polyala(1, 30, seed=21), pq.Params(stream=101), 120),
+            (pq.Topology.polyala(1, 64, seed=22), pq.Params(stream=102), 75),
+            (pq.Topology.polyala(1, 110, seed=23), pq.Params(stream=103), 200)]
+
+
+@pytest.mark.gpu
+def test_batch_add_remove_mid_run_matches_alone(gpu, mix):
+    (ta, pa, _), (tb, pb, _), (tc, pc, _) = mix
+    xa, va = _alone(gpu, ta, pa, 300)
+    b = gpu.Batch(max_atoms=ta.n_atoms + tb.n_atoms + tc.n_atoms + 256, max_systems=4)
+    sa = b.add_system(ta, pa)
+    sb = b.add_system(tb, pb)
+    b.step(100)
+    b.remove_system(sb)
+    sc = b.add_system(tc, pc)  # reuses B's slot and part of its range
+    b.step(150)
+    sd = b.add_system(tb, gpu.Params(stream=104))
+    b.step(50)
+    x, v = b.get_state(sa)
+    assert b.timestep(sa) == 300 and b.timestep(sc) == 200 and b.timestep(sd) == 50
+    assert np.array_equal(x, xa) and np.array_equal(v, va)
+    # C joined at step 100 of A's run: its own 200 steps equal C alone
+    xc, vc = _alone(gpu, tc, pc, 200)
+    xcb, vcb = b.get_state(sc)
+    assert np.array_equal(xcb, xc) and np.array_equal(vcb, vc)
+    b.close()
+
+
+@pytest.mark.gpu
+def test_served_jobs_match_running_alone(gpu, mix):
+    # a long job first; the mix arrives while it is on the GPU
+    jobs = [(mix[2][0], gpu.Params(stream=105), 1500)] + list(mix)
+    ref = [_alone(gpu, t, p, n) for t, p, n in jobs]
+    with gpu.Server(1 << 30, chunk_steps=50) as srv:
+        ids = [srv.submit(jobs[0][0], jobs[0][2], jobs[0][1], tag=0)]
+        t_end = time.time() + 30
+        while srv.stats()["resident_jobs"] == 0 and time.time() < t_end:
+            time.sleep(0.001)
+        ids += [srv.submit(t, n, p, tag=k) for k, (t, p, n) in enumerate(jobs) if k > 0]
+        res = _drain(srv, len(ids))
+        st = srv.stats()
+    for k, jid in enumerate(ids):
+        r = res[jid]
+        assert r.ok, r.message
+        assert r.tag == k and r.steps_done == jobs[k][2] and r.n_atoms == jobs[k][0].n_atoms
+        assert r.submit_s <= r.start_s <= r.end_s
+        assert np.array_equal(r.positions, ref[k][0]) and np.array_equal(r.velocities, ref[k][1])
+    # the later jobs were admitted while the long one was resident (their work overlapped)
+    assert min(res[j].start_s for j in ids[1:]) < res[ids[0]].end_s
+    assert st["completed"] == len(jobs) and st["failed"] == 0
+    expect = sum(t.n_atoms * n for t, _, n in jobs)
+    assert abs(st["atom_steps"] - expect) < 0.5
+
+
+@pytest.mark.gpu
+def test_admission_waits_for_hbm_footprint(gpu, mix):
+    big = mix[2][0]
+    # an arena that holds one of these jobs but not two
+    probe = gpu.Server(1 << 28, max_systems=2)
+    per_atom = probe.stats()["device_bytes"] / max(probe.stats()["capacity_atoms"], 1)
+    probe.close()
+    budget = int(per_atom * (1.5 * big.n_atoms + 64 + 2 * 32))
+    ref = _alone(gpu, big, gpu.Params(stream=7), 60)
+    with gpu.Server(budget, max_systems=2, chunk_steps=20) as srv:
+        cap = srv.stats()["capacity_atoms"]
+        assert big.n_atoms <= cap < 2 * big.n_atoms
+        ids = [srv.submit(big, 60, gpu.Params(stream=7), tag=i) for i in range(3)]
+        res = _drain(srv, 3)
+    runs = sorted((res[j].start_s, res[j].end_s) for j in ids)
+    for (s0, e0), (s1, e1) in zip(runs, runs[1:]):
+        assert s1 >= e0 - 1e-6  # admitted only after the previous job left the arena
+    for j in ids:
+        assert res[j].ok, res[j].message
+        assert np.array_equal(res[j].positions, ref[0]) and np.array_equal(res[j].velocities, ref[1])
+
+
+@pytest.mark.gpu
+def test_oversized_job_rejected_at_submit(gpu, mix):
+    with gpu.Server(1 << 26, max_systems=4) as srv:
+        cap = srv.stats()["capacity_atoms"]
+        huge = gpu.Topology.polyala(1, cap // 10 + 8, seed=5)
+        with pytest.raises(gpu.PrismQError) as e:
+            srv.submit(huge, 10)
+        assert e.value.status == 4  # E_CAPACITY
+        jid = srv.submit(mix[0][0], 10, mix[0][1])
+        assert _drain(srv, 1)[jid].ok
+
+
+@pytest.mark.gpu
+def test_failing_job_does_not_disturb_the_others(gpu, mix, ala40):
+    (ta, pa, na), (tb, pb, nb) = mix[0], mix[1]
+    ref_a = _alone(gpu, ta, pa, na)
+    ref_b = _alone(gpu, tb, pb, nb)
+    bad = gpu.Params(max_constraint_iter=1, temperature=600.0, stream=9)
+    with gpu.Server(1 << 30, chunk_steps=25) as srv:
+        ia = srv.submit(ta, na, pa)
+        ix = srv.submit(ala40, 200, bad)
+        ib = srv.submit(tb, nb, pb)
+        res = _drain(srv, 3)
+    assert res[ix].status in (7, 8) and res[ix].steps_done < 200 and res[ix].message
+    for jid, ref in ((ia, ref_a), (ib, ref_b)):
+        assert res[jid].ok, res[jid].message
+        assert np.array_equal(res[jid].positions, ref[0]) and np.array_equal(res[jid].velocities, ref[1])
