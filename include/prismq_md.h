@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define PRISMQ_ABI_VERSION 1
+#define PRISMQ_ABI_VERSION 2
 
 typedef enum prismq_status {
   PRISMQ_OK = 0,
@@ -122,10 +122,20 @@ typedef struct prismq_params {
   int32_t max_constraint_iter;/* SHAKE/RATTLE iteration bound (100) */
   uint32_t seed;              /* Philox key word 0 */
   uint32_t stream;            /* Philox key word 1 (system id in a batch) */
+  float shake_tol;            /* SHAKE: |r^2 - L^2| / L^2 (shake_cluster_positions :1890, 1e-4; <= 0 selects it) */
+  float rattle_tol;           /* RATTLE: |r·v_rel| / (|r| max(|v_rel|, 1)) (:2176, 1e-5; <= 0 selects it) */
+  int32_t constraint_check_fp64; /* 1: constraint residuals and multipliers in FP64 (0: FP32 as the reference) */
+  int32_t precision;          /* prismq_precision of the run */
 } prismq_params;
 
+typedef enum prismq_precision {
+  PRISMQ_PRECISION_FP32 = 0,  /* production: FP32 math, int64 fixed-point forces */
+  PRISMQ_PRECISION_FP64 = 1   /* precision study: FP64 state, forces and integrator everywhere */
+} prismq_precision;
+
 /* Fill *p with the reference engine defaults under HMR
- * (dt 0.004, T 300, γ 1, cutoff 10, skin 2, rebuild 20, COM 100, 100 iterations). */
+ * (dt 0.004, T 300, γ 1, cutoff 10, skin 2, rebuild 20, COM 100, 100 iterations,
+ * SHAKE 1e-4, RATTLE 1e-5, FP32 constraint checks, FP32 precision). */
 void prismq_params_default(prismq_params* p);
 
 const char* prismq_last_error(void);
@@ -189,6 +199,13 @@ prismq_status prismq_compute_forces(prismq_system* sys, double* pe_total, float*
                                     int64_t* f_fixed);
 /* Energy components: [bond, angle, dihedral, exception, nonbonded(shifted), kinetic]. */
 prismq_status prismq_energy_components(prismq_system* sys, double out[6]);
+/* Virial tensor W_ab = Σ_i x_a F_b (kcal/mol, row-major [9]) at the current
+ * positions, reduced in FP64. */
+prismq_status prismq_virial(prismq_system* sys, double out[9]);
+/* FP64 state and forces (FP64 systems hold them natively; FP32 systems return
+ * their FP32 values widened).  double[3N] each; forces at the last evaluation. */
+prismq_status prismq_get_state_f64(prismq_system* sys, double* xyz, double* vxyz);
+prismq_status prismq_get_forces_f64(prismq_system* sys, double* f);
 
 /* Build the pair list at the current positions and return the canonical
  * (i<j) pairs, sorted, as int32 pairs_out[2*n].  REF27 reproduces the
@@ -221,6 +238,10 @@ typedef struct prismq_batch prismq_batch;
 
 /* Create an empty batch with room for max_atoms atoms in total. */
 prismq_status prismq_batch_create(int64_t max_atoms, int32_t max_systems, prismq_batch** out);
+/* Same, for systems of one precision (prismq_precision); every system added
+ * must carry params.precision equal to it. */
+prismq_status prismq_batch_create_ex(int64_t max_atoms, int32_t max_systems, int32_t precision,
+                                     prismq_batch** out);
 void prismq_batch_destroy(prismq_batch* b);
 /* Admit a system; *slot receives its index.  PRISMQ_E_CAPACITY if it does not fit. */
 prismq_status prismq_batch_add_system(prismq_batch* b, const prismq_topology* topo,
@@ -241,6 +262,9 @@ prismq_status prismq_batch_tuning(prismq_batch* b, int32_t out[3]);
 /* out[0] = steps taken, out[1] = neighbour-list builds so far. */
 prismq_status prismq_batch_counters(prismq_batch* b, int32_t slot, int64_t out[2]);
 prismq_status prismq_batch_energy(prismq_batch* b, int32_t slot, double out[6]);
+prismq_status prismq_batch_virial(prismq_batch* b, int32_t slot, double out[9]);
+prismq_status prismq_batch_get_state_f64(prismq_batch* b, int32_t slot, double* xyz, double* vxyz);
+prismq_status prismq_batch_get_forces_f64(prismq_batch* b, int32_t slot, double* f);
 int64_t prismq_batch_resident_atoms(const prismq_batch* b);
 /* Whole-arena state transfer: float[3*span] in arena atom order (span =
  * prismq_batch_atom_span; system `slot` starts at prismq_batch_atom_offset).

@@ -60,6 +60,7 @@ def lib() -> ctypes.CDLL:
         L.orc_get_state.argtypes = [P, P, P]
         L.orc_forces_ref_f32.argtypes = [P, P, P, ctypes.c_int]
         L.orc_forces_f64.argtypes = [P, P, P, ctypes.c_int]
+        L.orc_forces_f64_rule.argtypes = [P, P, P, ctypes.c_int, ctypes.c_int]
         L.orc_phases.argtypes = [P, ctypes.c_int, P, ctypes.c_longlong]
         L.orc_com_remove.argtypes = [P]
         L.orc_run.argtypes = [P, ctypes.c_long, ctypes.c_int]
@@ -174,10 +175,12 @@ class OracleSystem:
             raise RuntimeError(f"oracle force error {rc}")
         return f, e
 
-    def forces_f64(self, threads: int = 0):
+    def forces_f64(self, threads: int = 0, incl64: bool = False):
+        """FP64 forces and energies; pairs enter by the FP32 r^2 rule, or by r^2
+        in double with incl64 (the pair set of an FP64-everywhere run)."""
         f = np.zeros((self.n, 3), dtype=np.float64)
         e = np.zeros(5, dtype=np.float64)
-        lib().orc_forces_f64(self.h, _ptr(f), _ptr(e), threads)
+        lib().orc_forces_f64_rule(self.h, _ptr(f), _ptr(e), threads, 1 if incl64 else 0)
         return f, e
 
     def phases(self, which: int, f_fixed: np.ndarray, step: int) -> int:

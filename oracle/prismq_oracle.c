@@ -845,6 +845,13 @@ static void dihedral_f64(const double* x, const prismq_dihedral* t, double f0[3]
 }
 
 int orc_forces_f64(orc_sys* s, double* f, double* e5, int threads) {
+  return orc_forces_f64_rule(s, f, e5, threads, 0);
+}
+
+/* incl64 = 0: ordinary pairs enter by the FP32 r^2 rule of the FP32 kernels
+ * (the pair set the production path evaluates); incl64 = 1: by r^2 in double
+ * (the pair set of the FP64-everywhere run). */
+int orc_forces_f64_rule(orc_sys* s, double* f, double* e5, int threads, int incl64) {
 #ifdef _OPENMP
   if (threads > 0) omp_set_num_threads(threads);
 #else
@@ -920,13 +927,17 @@ int orc_forces_f64(orc_sys* s, double* f, double* e5, int threads) {
           for (int k = start[cc]; k < start[cc + 1]; ++k) {
             const int j = mem[k];
             if (j == i) continue;
-            float df[3];
-            const float r2f = r2_force(s->x, i, j, df);
-            if (r2f >= cut2 || r2f < 0.01f) continue;
-            if (excluded(i, j, s->all_off, s->all_list)) continue;
             double d[3];
             for (int q = 0; q < 3; ++q) d[q] = xd[3 * j + q] - xd[3 * i + q];
             const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+            if (incl64) {
+              if (r2 >= (double)cut2 || r2 < (double)0.01f) continue;
+            } else {
+              float df[3];
+              const float r2f = r2_force(s->x, i, j, df);
+              if (r2f >= cut2 || r2f < 0.01f) continue;
+            }
+            if (excluded(i, j, s->all_off, s->all_list)) continue;
             const double inv_r = 1.0 / sqrt(r2), inv_r2 = inv_r * inv_r;
             const double sigma = 0.5 * ((double)s->sig[i] + (double)s->sig[j]);
             const double eps = sqrt((double)s->eps[i] * (double)s->eps[j]);

@@ -69,6 +69,7 @@ int orc_forces_ref_f32(orc_sys* s, float* f, double* e5, int threads);
  * r2 < cutoff^2 and >= 0.01, exclusions and exception pairs removed), all
  * arithmetic in double. */
 int orc_forces_f64(orc_sys* s, double* f, double* e5, int threads);
+int orc_forces_f64_rule(orc_sys* s, double* f, double* e5, int threads, int incl64);
 
 /* Integrator phase sets on the current state with forces given as int64
  * fixed point (2^-32 kcal/mol/Å).  set 1 = OU½, RATTLE, KICK½, RATTLE, DRIFT,

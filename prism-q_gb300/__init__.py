@@ -27,6 +27,7 @@ STATUS = {
     11: "E_NOT_FOUND",
 }
 NLIST_COMPLETE, NLIST_REF27 = 0, 1
+PRECISION_FP32, PRECISION_FP64 = 0, 1
 PHASES_PRE, PHASES_POST = 1, 2
 
 
@@ -79,7 +80,9 @@ class ParamsStruct(ctypes.Structure):
     _fields_ = [("dt", ctypes.c_float), ("temperature", ctypes.c_float), ("gamma", ctypes.c_float),
                 ("cutoff", ctypes.c_float), ("skin", ctypes.c_float), ("rebuild_interval", ctypes.c_int32),
                 ("com_interval", ctypes.c_int32), ("max_constraint_iter", ctypes.c_int32),
-                ("seed", ctypes.c_uint32), ("stream", ctypes.c_uint32)]
+                ("seed", ctypes.c_uint32), ("stream", ctypes.c_uint32),
+                ("shake_tol", ctypes.c_float), ("rattle_tol", ctypes.c_float),
+                ("constraint_check_fp64", ctypes.c_int32), ("precision", ctypes.c_int32)]
 
 
 class ServerConfigStruct(ctypes.Structure):
@@ -172,6 +175,13 @@ def load() -> ctypes.CDLL:
         "prismq_batch_run_timed": (I, [P, i64, P, P]),
         "prismq_batch_counters": (I, [P, ctypes.c_int32, P]),
         "prismq_batch_tuning": (I, [P, P]),
+        "prismq_batch_create_ex": (I, [i64, ctypes.c_int32, ctypes.c_int32, P]),
+        "prismq_batch_virial": (I, [P, ctypes.c_int32, P]),
+        "prismq_batch_get_state_f64": (I, [P, ctypes.c_int32, P, P]),
+        "prismq_batch_get_forces_f64": (I, [P, ctypes.c_int32, P]),
+        "prismq_virial": (I, [P, P]),
+        "prismq_get_state_f64": (I, [P, P, P]),
+        "prismq_get_forces_f64": (I, [P, P]),
         "prismq_server_config_default": (None, [P]),
         "prismq_server_create": (I, [i64, P, P]),
         "prismq_server_submit": (I, [P, P, P]),
@@ -224,11 +234,16 @@ class Params:
     max_constraint_iter: int = 100
     seed: int = 0x50524953
     stream: int = 0
+    shake_tol: float = 1e-4           # |r^2 - L^2| / L^2 (reference value)
+    rattle_tol: float = 1e-5          # relative velocity residual (reference value)
+    constraint_check_fp64: bool = False
+    precision: int = PRECISION_FP32   # PRECISION_FP64: FP64 state, forces and integrator
 
     def struct(self) -> ParamsStruct:
         return ParamsStruct(self.dt, self.temperature, self.gamma, self.cutoff, self.skin,
                             self.rebuild_interval, self.com_interval, self.max_constraint_iter,
-                            self.seed & 0xffffffff, self.stream & 0xffffffff)
+                            self.seed & 0xffffffff, self.stream & 0xffffffff, self.shake_tol, self.rattle_tol,
+                            1 if self.constraint_check_fp64 else 0, int(self.precision))
 
 
 # ---------------------------------------------------------------- topology
@@ -404,6 +419,25 @@ class NhsAmberFusedEngine:
         _check(load().prismq_energy_components(self.h, _ptr(out)))
         return out
 
+    def virial(self) -> np.ndarray:
+        """W_ab = sum_i x_a F_b (3x3, kcal/mol), reduced in FP64."""
+        out = np.zeros(9, np.float64)
+        _check(load().prismq_virial(self.h, _ptr(out)))
+        return out.reshape(3, 3)
+
+    def get_state_f64(self):
+        """(positions, velocities) as float64 [N,3] (native for FP64 systems)."""
+        x = np.zeros((self.n_atoms, 3), np.float64)
+        v = np.zeros((self.n_atoms, 3), np.float64)
+        _check(load().prismq_get_state_f64(self.h, _ptr(x), _ptr(v)))
+        return x, v
+
+    def get_forces_f64(self) -> np.ndarray:
+        """Forces of the last evaluation as float64 [N,3]."""
+        f = np.zeros((self.n_atoms, 3), np.float64)
+        _check(load().prismq_get_forces_f64(self.h, _ptr(f)))
+        return f
+
     def build_neighbors(self, mode: int = NLIST_COMPLETE) -> np.ndarray:
         n = ctypes.c_size_t()
         L = load()
@@ -424,9 +458,9 @@ class NhsAmberFusedEngine:
 class Batch:
     """Many independent systems advanced together in one launch per phase."""
 
-    def __init__(self, max_atoms: int, max_systems: int):
+    def __init__(self, max_atoms: int, max_systems: int, precision: int = PRECISION_FP32):
         self.h = ctypes.c_void_p()
-        _check(load().prismq_batch_create(max_atoms, max_systems, ctypes.byref(self.h)))
+        _check(load().prismq_batch_create_ex(max_atoms, max_systems, precision, ctypes.byref(self.h)))
         self.n_atoms: dict[int, int] = {}
         self._keep: dict[int, tuple] = {}
 
@@ -492,6 +526,25 @@ class Batch:
         out = np.zeros(6, np.float64)
         _check(load().prismq_batch_energy(self.h, slot, _ptr(out)))
         return out
+
+    def virial(self, slot: int) -> np.ndarray:
+        """W_ab = sum_i x_a F_b (3x3, kcal/mol) at the current positions."""
+        out = np.zeros(9, np.float64)
+        _check(load().prismq_batch_virial(self.h, slot, _ptr(out)))
+        return out.reshape(3, 3)
+
+    def get_state_f64(self, slot: int):
+        n = self.n_atoms[slot]
+        x = np.zeros((n, 3), np.float64)
+        v = np.zeros((n, 3), np.float64)
+        _check(load().prismq_batch_get_state_f64(self.h, slot, _ptr(x), _ptr(v)))
+        return x, v
+
+    def forces_f64(self, slot: int) -> np.ndarray:
+        """Forces of the last evaluation (kcal/mol/Å) as float64."""
+        f = np.zeros((self.n_atoms[slot], 3), np.float64)
+        _check(load().prismq_batch_get_forces_f64(self.h, slot, _ptr(f)))
+        return f
 
     @property
     def resident_atoms(self) -> int:

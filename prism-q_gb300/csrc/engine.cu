@@ -109,6 +109,7 @@ struct Lowered {
   int n = 0;
   std::vector<float4> pos, vel;
   std::vector<float2> lj;
+  std::vector<double2> lj64;  // the same in double (FP64 batches)
   std::vector<unsigned long long> mask_all, mask_ref;
   std::vector<int2> far;
   std::vector<int> far_list;
@@ -141,6 +142,7 @@ prismq_status lower_topology(const prismq_topology* T, Lowered* L) {
   L->pos.resize(n);
   L->vel.resize(n);
   L->lj.resize(n);
+  L->lj64.resize(n);
   L->charges.assign(T->charges, T->charges + n);
   L->masses.assign(T->masses, T->masses + n);
   for (int a = 0; a < n; ++a) {
@@ -157,6 +159,7 @@ prismq_status lower_topology(const prismq_topology* T, Lowered* L) {
     L->pos[a] = make_float4(x, y, z, T->charges[a]);
     L->vel[a] = make_float4(0.f, 0.f, 0.f, m);
     L->lj[a] = make_float2(0.5f * sg, sqrtf(ep));
+    L->lj64[a] = make_double2(0.5 * (double)sg, std::sqrt((double)ep));
   }
   auto in_range = [n](int i) { return i >= 0 && i < n; };
   // ---- bonded terms + incidence ----
@@ -368,6 +371,12 @@ prismq_status check_params(const prismq_params* p) {
   if (p->rebuild_interval < 1) return fail(PRISMQ_E_INVALID, "rebuild_interval must be >= 1");
   if (p->max_constraint_iter < 1) return fail(PRISMQ_E_INVALID, "max_constraint_iter must be >= 1");
   if (p->com_interval < 0) return fail(PRISMQ_E_INVALID, "com_interval must be >= 0");
+  if (!std::isfinite(p->shake_tol) || !std::isfinite(p->rattle_tol))
+    return fail(PRISMQ_E_INVALID, "constraint tolerances must be finite");
+  if (p->constraint_check_fp64 != 0 && p->constraint_check_fp64 != 1)
+    return fail(PRISMQ_E_INVALID, "constraint_check_fp64 must be 0 or 1");
+  if (p->precision != PRISMQ_PRECISION_FP32 && p->precision != PRISMQ_PRECISION_FP64)
+    return fail(PRISMQ_E_INVALID, "unknown precision");
   return PRISMQ_OK;
 }
 
@@ -388,6 +397,10 @@ void fill_params(SysDev* S, const prismq_params& p) {
   S->max_iter = p.max_constraint_iter;
   S->seed = p.seed;
   S->stream = p.stream;
+  S->shake_tol = p.shake_tol > 0.f ? p.shake_tol : 1.0e-4f;
+  S->rattle_tol = p.rattle_tol > 0.f ? p.rattle_tol : 1.0e-5f;
+  S->check64 = p.constraint_check_fp64;
+  S->c1d = std::exp(-(double)p.gamma * 0.5 * (double)p.dt);
 }
 
 // ---------------------------------------------------------------------------
@@ -407,10 +420,32 @@ __global__ void k_xyz_to_aos(float* dst, const float4* src, int n) {
   dst[3 * i + 1] = v.y;
   dst[3 * i + 2] = v.z;
 }
+__global__ void k_aos_to_xyz64(double4_32a* dst, const float* src, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double4_32a o = dst[i];
+  dst[i] = make_double4_32a(src[3 * i], src[3 * i + 1], src[3 * i + 2], o.w);
+}
+__global__ void k_xyz64_to_aos(double* dst, const double4_32a* src, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double4_32a v = src[i];
+  dst[3 * i] = v.x;
+  dst[3 * i + 1] = v.y;
+  dst[3 * i + 2] = v.z;
+}
+__global__ void k_xyz_to_aos64(double* dst, const float4* src, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 v = src[i];
+  dst[3 * i] = v.x;
+  dst[3 * i + 1] = v.y;
+  dst[3 * i + 2] = v.z;
+}
 // Whole-arena state upload: positions whose bits change mark their system for
 // a force/list refresh before the next step.
-__global__ void k_set_state_all(float4* pos, float4* vel, const float* xs, const float* vs, const int* atom_sys,
-                                SysDev* sys, int64_t n) {
+__global__ void k_set_state_all(float4* pos, float4* vel, double4_32a* pos64, double4_32a* vel64, const float* xs,
+                                const float* vs, const int* atom_sys, SysDev* sys, int64_t n) {
   const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= n) return;
   const int s = atom_sys[a];
@@ -421,12 +456,14 @@ __global__ void k_set_state_all(float4* pos, float4* vel, const float* xs, const
     if (__float_as_uint(x) != __float_as_uint(o.x) || __float_as_uint(y) != __float_as_uint(o.y) ||
         __float_as_uint(z) != __float_as_uint(o.z)) {
       pos[a] = make_float4(x, y, z, o.w);
+      if (pos64) pos64[a] = make_double4_32a(x, y, z, pos64[a].w);
       atomicOr(&sys[s].need_prime, 1);
     }
   }
   if (vs) {
     const float4 o = vel[a];
     vel[a] = make_float4(vs[3 * a], vs[3 * a + 1], vs[3 * a + 2], o.w);
+    if (vel64) vel64[a] = make_double4_32a(vs[3 * a], vs[3 * a + 1], vs[3 * a + 2], vel64[a].w);
   }
 }
 __global__ void k_get_state_all(const float4* pos, const float4* vel, float* xs, float* vs, int64_t n) {
@@ -476,9 +513,12 @@ struct prismq_batch {
   int sys_span = 0;
   int force_variant = -1;  // autotuned launch shape of the force kernel
   int64_t tuned_span = -1;
-  double* d_energy = nullptr;
+  double* d_energy = nullptr;  // kEnergyOut per system
   float* d_stage = nullptr;
   float* d_stage2 = nullptr;
+  double* d_stage64 = nullptr;  // allocated on first FP64 read-back
+  int precision = PRISMQ_PRECISION_FP32;
+  int n_check32 = 0, n_check64 = 0;  // resident FP32 systems by constraint-check precision
   std::vector<SysDev> h_sys;
 
   ~prismq_batch() {
@@ -486,7 +526,7 @@ struct prismq_batch {
     void* ptrs[] = {A.pos, A.vel, A.lj, A.xref, A.f, A.pe, A.atom_sys, A.mask_all, A.mask_ref, A.far,
                     A.far_list, A.inc, A.inc_list, A.ex_idx, A.ex_partner, A.ex_par, A.bonds, A.angles,
                     A.dihs, A.units, A.nbr, A.nnbr, A.cell_start, A.cell_atoms, A.atom_cell, A.work, A.work_ctl, A.sys,
-                    d_energy, d_stage, d_stage2};
+                    A.pos64, A.vel64, A.f64, A.lj64, d_energy, d_stage, d_stage2, d_stage64};
     for (void* p : ptrs)
       if (p) cudaFree(p);
     if (st) cudaStreamDestroy(st);
@@ -495,9 +535,16 @@ struct prismq_batch {
   void update_spans() {
     const int64_t na = r_atoms.high(), nu = r_units.high();
     int ns = 0;
+    int c32 = 0, c64 = 0;
     for (int i = 0; i < (int)slots.size(); ++i)
-      if (slots[i].active) ns = i + 1;
+      if (slots[i].active) {
+        ns = i + 1;
+        (slots[i].params.constraint_check_fp64 ? c64 : c32) += 1;
+      }
     if (na != atom_span || nu != unit_span || ns != sys_span) graph_dirty = true;
+    if ((c32 > 0) != (n_check32 > 0) || (c64 > 0) != (n_check64 > 0)) graph_dirty = true;
+    n_check32 = c32;
+    n_check64 = c64;
     atom_span = na;
     unit_span = nu;
     sys_span = ns;
@@ -509,6 +556,27 @@ struct prismq_batch {
     PQ_CK(cudaStreamSynchronize(st));
     return PRISMQ_OK;
   }
+
+  // The integrate launch(es) of one step: FP64 batches run one pass; FP32
+  // batches run one pass per constraint-check precision present.  Returns the
+  // number of kernels launched.
+  int integrate(int mode) {
+    if (A.fp64) {
+      launch_integrate(A, unit_span, mode, st, 0);
+      return 1;
+    }
+    int k = 0;
+    if (n_check32 > 0 || n_check64 == 0) {
+      launch_integrate(A, unit_span, mode, st, 0);
+      ++k;
+    }
+    if (n_check64 > 0) {
+      launch_integrate(A, unit_span, mode, st, 1);
+      ++k;
+    }
+    return k;
+  }
+  int integrate_passes() const { return A.fp64 ? 1 : (n_check32 > 0 || n_check64 == 0 ? 1 : 0) + (n_check64 > 0 ? 1 : 0); }
 
   void enqueue_step_body() {
     launch_control_cells(A, sys_span, kCtlStep, -1, st);
@@ -561,7 +629,7 @@ struct prismq_batch {
     cudaGraph_t g;
     PQ_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     enqueue_step_body();
-    launch_integrate(A, unit_span, kIntBoth, st);
+    integrate(kIntBoth);
     PQ_CK(cudaStreamEndCapture(st, &g));
     cudaError_t e = cudaGraphInstantiate(&gexec, g, 0);
     cudaGraphDestroy(g);
@@ -622,8 +690,7 @@ struct prismq_batch {
     if ((rc = tune_force()) != PRISMQ_OK) return rc;
     std::vector<cudaEvent_t> ev(4 * n + 1);
     for (auto& e : ev) PQ_CK(cudaEventCreate(&e));
-    launch_integrate(A, unit_span, kIntPre, st);
-    g_launches += 1;
+    g_launches += integrate(kIntPre);
     cudaGraph_t g;
     cudaGraphExec_t ge = nullptr;
     PQ_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -635,7 +702,7 @@ struct prismq_batch {
       cudaEventRecordWithFlags(ev[4 * i + 2], st, cudaEventRecordExternal);
       launch_force(A, atom_span, false, st, false, force_variant);
       cudaEventRecordWithFlags(ev[4 * i + 3], st, cudaEventRecordExternal);
-      launch_integrate(A, unit_span, kIntBoth, st);
+      integrate(kIntBoth);
     }
     cudaEventRecordWithFlags(ev[4 * n], st, cudaEventRecordExternal);
     PQ_CK(cudaStreamEndCapture(st, &g));
@@ -647,7 +714,7 @@ struct prismq_batch {
     cudaError_t le = cudaGraphLaunch(ge, st);
     nvtxRangePop();
     PQ_CK(le);
-    g_launches += 4 * n;
+    g_launches += (3 + integrate_passes()) * n;
     PQ_CK(cudaStreamSynchronize(st));
     PQ_CK(cudaEventElapsedTime(total_ms, ev[0], ev[4 * n]));
     if (phase_ms)
@@ -655,8 +722,7 @@ struct prismq_batch {
     cudaGraphExecDestroy(ge);
     for (auto& x : ev) cudaEventDestroy(x);
     enqueue_step_body();
-    launch_integrate(A, unit_span, kIntPost, st);
-    g_launches += 4;
+    g_launches += 3 + integrate(kIntPost);
     PQ_CK(cudaGetLastError());
     return check_status();
   }
@@ -668,15 +734,14 @@ struct prismq_batch {
     if (rc != PRISMQ_OK) return rc;
     rc = ensure_graph();
     if (rc != PRISMQ_OK) return rc;
-    launch_integrate(A, unit_span, kIntPre, st);
-    g_launches += 1;
+    g_launches += integrate(kIntPre);
+    const int per_step = 3 + integrate_passes();
     for (int64_t i = 1; i < n; ++i) {
       PQ_CK(cudaGraphLaunch(gexec, st));
-      g_launches += 4;
+      g_launches += per_step;
     }
     enqueue_step_body();
-    launch_integrate(A, unit_span, kIntPost, st);
-    g_launches += 4;
+    g_launches += 3 + integrate(kIntPost);
     PQ_CK(cudaGetLastError());
     return check_status();
   }
@@ -693,7 +758,8 @@ namespace {
 // receives the device bytes the same call would allocate.
 prismq_status batch_alloc(prismq_batch* B, int64_t atom_cap, int sys_cap, int64_t bond_cap,
                           int64_t angle_cap, int64_t dih_cap, int64_t inc_cap, int64_t ex_cap,
-                          int64_t far_cap, int64_t cell_cap, bool dry = false, int64_t* bytes_out = nullptr) {
+                          int64_t far_cap, int64_t cell_cap, int precision = PRISMQ_PRECISION_FP32,
+                          bool dry = false, int64_t* bytes_out = nullptr) {
   int ndev = 0;
   if (!dry && (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)) {
     cudaGetLastError();
@@ -747,12 +813,21 @@ prismq_status batch_alloc(prismq_batch* B, int64_t atom_cap, int sys_cap, int64_
   PQ_ALLOC(A.work, atom_cap / 8 + sys_cap + 1);
   PQ_ALLOC(A.work_ctl, 4);
   PQ_ALLOC(A.sys, sys_cap);
-  PQ_ALLOC(B->d_energy, 6 * (int64_t)sys_cap);
+  PQ_ALLOC(B->d_energy, kEnergyOut * (int64_t)sys_cap);
+  if (precision == PRISMQ_PRECISION_FP64) {
+    PQ_ALLOC(A.pos64, atom_cap);
+    PQ_ALLOC(A.vel64, atom_cap);
+    PQ_ALLOC(A.f64, 3 * atom_cap);
+    PQ_ALLOC(A.lj64, atom_cap);
+  }
   PQ_ALLOC(B->d_stage, 3 * atom_cap);
   PQ_ALLOC(B->d_stage2, 3 * atom_cap);
 #undef PQ_ALLOC
   if (bytes_out) *bytes_out = total;
   if (dry) return PRISMQ_OK;
+  B->precision = precision;
+  A.fp64 = precision == PRISMQ_PRECISION_FP64 ? 1 : 0;
+  if (A.fp64) PQ_CK(cudaMemsetAsync(A.f64, 0, sizeof(double) * 3 * atom_cap, B->st));
   PQ_CK(cudaMemsetAsync(A.sys, 0, sizeof(SysDev) * sys_cap, B->st));
   PQ_CK(cudaMemsetAsync(A.nnbr, 0, sizeof(int) * atom_cap, B->st));
   PQ_CK(cudaMemsetAsync(A.work_ctl, 0, sizeof(int) * 4, B->st));
@@ -781,10 +856,10 @@ prismq_status batch_alloc(prismq_batch* B, int64_t atom_cap, int sys_cap, int64_
 // 2/atom, angles 4, torsion terms 8, incidence entries 48, exceptions 8, far
 // exclusions 2) and every system may pad its atom range to 32.
 prismq_status batch_alloc_sized(prismq_batch* B, int64_t max_atoms, int32_t max_systems, bool dry,
-                                int64_t* bytes_out) {
+                                int64_t* bytes_out, int precision = PRISMQ_PRECISION_FP32) {
   const int64_t na = (max_atoms + 31) / 32 * 32 + 32 * (int64_t)max_systems;
   return batch_alloc(B, na, max_systems, 2 * na, 4 * na, 8 * na, 48 * na, 8 * na, 2 * na,
-                     2 * (na / 2 + 1026 * (int64_t)max_systems), dry, bytes_out);
+                     2 * (na / 2 + 1026 * (int64_t)max_systems), precision, dry, bytes_out);
 }
 
 template <class T>
@@ -802,6 +877,8 @@ prismq_status batch_admit(prismq_batch* B, const Lowered& L0, const prismq_param
       break;
     }
   if (slot < 0) return fail(PRISMQ_E_CAPACITY, "batch has no free system slot");
+  if (p.precision != B->precision)
+    return fail(PRISMQ_E_INVALID, "params.precision differs from the batch's precision");
   Lowered L = L0;
   SlotRec R;
   R.n_atoms = L.n;
@@ -894,6 +971,18 @@ prismq_status batch_admit(prismq_batch* B, const Lowered& L0, const prismq_param
   PQ_UP(A.dihs + R.dih_b, L.dihs);
   PQ_UP(A.units + R.unit_b, L.units);
 #undef PQ_UP
+  if (A.fp64) {
+    std::vector<double4_32a> p64(L.n), v64(L.n);
+    for (int a = 0; a < L.n; ++a) {
+      p64[a] = make_double4_32a(L.pos[a].x, L.pos[a].y, L.pos[a].z, L.pos[a].w);
+      v64[a] = make_double4_32a(L.vel[a].x, L.vel[a].y, L.vel[a].z, L.vel[a].w);
+    }
+    if ((rc = upload(A.pos64 + ab, p64, st)) != PRISMQ_OK) return rc;
+    if ((rc = upload(A.vel64 + ab, v64, st)) != PRISMQ_OK) return rc;
+    if ((rc = upload(A.lj64 + ab, L.lj64, st)) != PRISMQ_OK) return rc;
+    for (int c = 0; c < 3; ++c) PQ_CK(cudaMemsetAsync(A.f64 + c * A.atom_cap + ab, 0, sizeof(double) * L.n, st));
+    PQ_CK(cudaStreamSynchronize(st));  // the host staging vectors die here
+  }
   PQ_CK(cudaMemsetAsync(A.nnbr + ab, 0, sizeof(int) * L.n, st));
   PQ_CK(cudaMemsetAsync(A.f + ab, 0, sizeof(long long) * L.n, st));
   PQ_CK(cudaMemsetAsync(A.f + A.atom_cap + ab, 0, sizeof(long long) * L.n, st));
@@ -969,6 +1058,10 @@ prismq_status set_xyz(prismq_batch* B, int slot, float4* dst_plane, const float*
     if (!std::isfinite(in[i])) return fail(PRISMQ_E_INVALID, "non-finite input value");
   PQ_CK(cudaMemcpyAsync(B->d_stage, in, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, B->st));
   k_aos_to_xyz<<<(n + 255) / 256, 256, 0, B->st>>>(dst_plane + R.atom_b, B->d_stage, n);
+  if (B->A.fp64) {  // the FP64 state takes the same values
+    double4_32a* d64 = dst_plane == B->A.pos ? B->A.pos64 : B->A.vel64;
+    k_aos_to_xyz64<<<(n + 255) / 256, 256, 0, B->st>>>(d64 + R.atom_b, B->d_stage, n);
+  }
   PQ_CK(cudaGetLastError());
   PQ_CK(cudaStreamSynchronize(B->st));
   return PRISMQ_OK;
@@ -991,7 +1084,7 @@ prismq_status check_slot(prismq_batch* B, int slot) {
 
 // Forces + per-atom energy planes at the current positions; returns the
 // system's energy totals in out6 (host) when non-NULL.
-prismq_status eval_energy(prismq_batch* B, int slot, double* out6) {
+prismq_status eval_energy(prismq_batch* B, int slot, double* out15) {
   prismq_status rc = B->prime_if_needed();
   if (rc != PRISMQ_OK) return rc;
   launch_force(B->A, B->atom_span, true, B->st);
@@ -1000,8 +1093,9 @@ prismq_status eval_energy(prismq_batch* B, int slot, double* out6) {
   launch_force(B->A, B->atom_span, false, B->st);
   g_launches += 3;
   PQ_CK(cudaGetLastError());
-  if (out6) {
-    PQ_CK(cudaMemcpyAsync(out6, B->d_energy + 6 * slot, sizeof(double) * 6, cudaMemcpyDeviceToHost, B->st));
+  if (out15) {
+    PQ_CK(cudaMemcpyAsync(out15, B->d_energy + kEnergyOut * slot, sizeof(double) * kEnergyOut,
+                          cudaMemcpyDeviceToHost, B->st));
   }
   PQ_CK(cudaStreamSynchronize(B->st));
   return B->check_status(slot);
@@ -1038,6 +1132,10 @@ void prismq_params_default(prismq_params* p) {
   p->max_constraint_iter = 100;
   p->seed = 0x50524953u;
   p->stream = 0u;
+  p->shake_tol = 1.0e-4f;
+  p->rattle_tol = 1.0e-5f;
+  p->constraint_check_fp64 = 0;
+  p->precision = PRISMQ_PRECISION_FP32;
 }
 
 void prismq_debug_noise(uint32_t seed, uint32_t stream, uint32_t atom, uint64_t step, uint32_t purpose,
@@ -1069,9 +1167,15 @@ void prismq_topology_free(prismq_topology_buf* buf) { delete buf; }
 // ---- batch ----
 
 prismq_status prismq_batch_create(int64_t max_atoms, int32_t max_systems, prismq_batch** out) {
+  return prismq_batch_create_ex(max_atoms, max_systems, PRISMQ_PRECISION_FP32, out);
+}
+
+prismq_status prismq_batch_create_ex(int64_t max_atoms, int32_t max_systems, int32_t precision, prismq_batch** out) {
   if (!out || max_atoms <= 0 || max_systems <= 0) return fail(PRISMQ_E_INVALID, "invalid batch size");
+  if (precision != PRISMQ_PRECISION_FP32 && precision != PRISMQ_PRECISION_FP64)
+    return fail(PRISMQ_E_INVALID, "unknown precision");
   auto* B = new prismq_batch();
-  prismq_status rc = batch_alloc_sized(B, max_atoms, max_systems, false, nullptr);
+  prismq_status rc = batch_alloc_sized(B, max_atoms, max_systems, false, nullptr, precision);
   if (rc != PRISMQ_OK) {
     delete B;
     return rc;
@@ -1162,10 +1266,67 @@ prismq_status prismq_batch_status(prismq_batch* b, int32_t slot) {
   return b->check_status(slot);
 }
 
+prismq_status prismq_batch_virial(prismq_batch* b, int32_t slot, double out[9]) {
+  prismq_status rc = check_slot(b, slot);
+  if (rc != PRISMQ_OK) return rc;
+  if (!out) return fail(PRISMQ_E_INVALID, "out is NULL");
+  double e[kEnergyOut];
+  rc = eval_energy(b, slot, e);
+  if (rc != PRISMQ_OK) return rc;
+  for (int i = 0; i < 9; ++i) out[i] = e[6 + i];
+  return PRISMQ_OK;
+}
+
+prismq_status prismq_batch_get_state_f64(prismq_batch* b, int32_t slot, double* xyz, double* vxyz) {
+  prismq_status rc = check_slot(b, slot);
+  if (rc != PRISMQ_OK) return rc;
+  const SlotRec& R = b->slots[slot];
+  const int n = (int)R.n_atoms;
+  if (!b->d_stage64) PQ_CK(cudaMalloc((void**)&b->d_stage64, sizeof(double) * 3 * b->A.atom_cap));
+  for (int w = 0; w < 2; ++w) {
+    double* out = w == 0 ? xyz : vxyz;
+    if (!out) continue;
+    if (b->A.fp64)
+      k_xyz64_to_aos<<<(n + 255) / 256, 256, 0, b->st>>>(b->d_stage64, (w == 0 ? b->A.pos64 : b->A.vel64) + R.atom_b, n);
+    else
+      k_xyz_to_aos64<<<(n + 255) / 256, 256, 0, b->st>>>(b->d_stage64, (w == 0 ? b->A.pos : b->A.vel) + R.atom_b, n);
+    PQ_CK(cudaGetLastError());
+    PQ_CK(cudaMemcpyAsync(out, b->d_stage64, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, b->st));
+    PQ_CK(cudaStreamSynchronize(b->st));
+  }
+  return PRISMQ_OK;
+}
+
+prismq_status prismq_batch_get_forces_f64(prismq_batch* b, int32_t slot, double* f) {
+  prismq_status rc = check_slot(b, slot);
+  if (rc != PRISMQ_OK) return rc;
+  if (!f) return fail(PRISMQ_E_INVALID, "f is NULL");
+  const SlotRec& R = b->slots[slot];
+  const int64_t n = R.n_atoms;
+  if (b->A.fp64) {
+    std::vector<double> h(3 * n);
+    for (int c = 0; c < 3; ++c)
+      PQ_CK(cudaMemcpyAsync(h.data() + c * n, b->A.f64 + c * b->A.atom_cap + R.atom_b, sizeof(double) * n,
+                            cudaMemcpyDeviceToHost, b->st));
+    PQ_CK(cudaStreamSynchronize(b->st));
+    for (int64_t a = 0; a < n; ++a)
+      for (int c = 0; c < 3; ++c) f[3 * a + c] = h[c * n + a];
+  } else {
+    std::vector<long long> h(3 * n);
+    for (int c = 0; c < 3; ++c)
+      PQ_CK(cudaMemcpyAsync(h.data() + c * n, b->A.f + c * b->A.atom_cap + R.atom_b, sizeof(long long) * n,
+                            cudaMemcpyDeviceToHost, b->st));
+    PQ_CK(cudaStreamSynchronize(b->st));
+    for (int64_t a = 0; a < n; ++a)
+      for (int c = 0; c < 3; ++c) f[3 * a + c] = (double)h[c * n + a] * kFixedInvD;
+  }
+  return PRISMQ_OK;
+}
+
 prismq_status prismq_batch_energy(prismq_batch* b, int32_t slot, double out[6]) {
   prismq_status rc = check_slot(b, slot);
   if (rc != PRISMQ_OK) return rc;
-  double e[6];
+  double e[kEnergyOut];
   rc = eval_energy(b, slot, e);
   if (rc != PRISMQ_OK) return rc;
   // five potential planes in order: bond, angle, dihedral, exception, nonbonded; then kinetic
@@ -1191,7 +1352,8 @@ prismq_status prismq_batch_set_state_all(prismq_batch* b, const float* xyz, cons
   if (n == 0) return PRISMQ_OK;
   if (xyz) PQ_CK(cudaMemcpyAsync(b->d_stage, xyz, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, b->st));
   if (vxyz) PQ_CK(cudaMemcpyAsync(b->d_stage2, vxyz, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, b->st));
-  k_set_state_all<<<(unsigned)((n + 255) / 256), 256, 0, b->st>>>(b->A.pos, b->A.vel, xyz ? b->d_stage : nullptr,
+  k_set_state_all<<<(unsigned)((n + 255) / 256), 256, 0, b->st>>>(b->A.pos, b->A.vel, b->A.pos64, b->A.vel64,
+                                                                   xyz ? b->d_stage : nullptr,
                                                                    vxyz ? b->d_stage2 : nullptr, b->A.atom_sys,
                                                                    b->A.sys, n);
   g_launches += 1;
@@ -1245,7 +1407,7 @@ prismq_status prismq_system_create(const prismq_topology* topo, const prismq_par
   const int64_t n = L.n;
   rc = batch_alloc(B, n, 1, (int64_t)L.bonds.size(), (int64_t)L.angles.size(), (int64_t)L.dihs.size(),
                    (int64_t)L.inc_list.size(), (int64_t)L.ex_partner.size(), (int64_t)L.far_list.size(),
-                   2 * ((int64_t)L.cell_cap + 1));
+                   2 * ((int64_t)L.cell_cap + 1), params->precision);
   if (rc != PRISMQ_OK) {
     delete B;
     return rc;
@@ -1334,11 +1496,22 @@ prismq_status prismq_step(prismq_system* sys, int64_t n_steps) {
 prismq_status prismq_compute_forces(prismq_system* sys, double* pe_total, float* f_aos, int64_t* f_fixed) {
   if (!sys) return fail(PRISMQ_E_INVALID, "system is NULL");
   prismq_batch* B = sys->b;
-  double e[6];
+  double e[kEnergyOut];
   prismq_status rc = eval_energy(B, sys->slot, e);
   if (rc != PRISMQ_OK) return rc;
   if (pe_total) *pe_total = e[0] + e[1] + e[2] + e[3] + e[4];
-  if (f_aos || f_fixed) {
+  if ((f_aos || f_fixed) && B->A.fp64) {
+    const int64_t n = B->slots[sys->slot].n_atoms;
+    std::vector<double> h(3 * n);
+    if ((rc = prismq_batch_get_forces_f64(B, sys->slot, h.data())) != PRISMQ_OK) return rc;
+    for (int64_t i = 0; i < 3 * n; ++i) {
+      if (f_aos) f_aos[i] = (float)h[i];
+      if (f_fixed) {
+        const double v = h[i] * 4294967296.0;
+        f_fixed[i] = !(v == v) ? 0 : v >= 9.2233720368547758e18 ? INT64_MAX : v <= -9.2233720368547758e18 ? INT64_MIN : (int64_t)std::llrint(v);
+      }
+    }
+  } else if (f_aos || f_fixed) {
     const SlotRec& R = B->slots[sys->slot];
     const int64_t n = R.n_atoms;
     std::vector<long long> h(3 * n);
@@ -1359,6 +1532,21 @@ prismq_status prismq_compute_forces(prismq_system* sys, double* pe_total, float*
 prismq_status prismq_energy_components(prismq_system* sys, double out[6]) {
   if (!sys || !out) return fail(PRISMQ_E_INVALID, "NULL argument");
   return prismq_batch_energy(sys->b, sys->slot, out);
+}
+
+prismq_status prismq_virial(prismq_system* sys, double out[9]) {
+  if (!sys || !out) return fail(PRISMQ_E_INVALID, "NULL argument");
+  return prismq_batch_virial(sys->b, sys->slot, out);
+}
+
+prismq_status prismq_get_state_f64(prismq_system* sys, double* xyz, double* vxyz) {
+  if (!sys) return fail(PRISMQ_E_INVALID, "system is NULL");
+  return prismq_batch_get_state_f64(sys->b, sys->slot, xyz, vxyz);
+}
+
+prismq_status prismq_get_forces_f64(prismq_system* sys, double* f) {
+  if (!sys) return fail(PRISMQ_E_INVALID, "system is NULL");
+  return prismq_batch_get_forces_f64(sys->b, sys->slot, f);
 }
 
 prismq_status prismq_build_neighbors(prismq_system* sys, prismq_nlist_mode mode, int32_t* pairs_out, size_t cap,
@@ -1414,6 +1602,7 @@ prismq_status prismq_debug_phases(prismq_system* sys, prismq_phase_set set, int6
   if (!sys) return fail(PRISMQ_E_INVALID, "system is NULL");
   if (set != PRISMQ_PHASES_PRE && set != PRISMQ_PHASES_POST) return fail(PRISMQ_E_INVALID, "unknown phase set");
   prismq_batch* B = sys->b;
+  if (B->A.fp64) return fail(PRISMQ_E_INVALID, "single phase sets are an FP32 parity entry point");
   prismq_status rc = B->prime_if_needed();
   if (rc != PRISMQ_OK) return rc;
   launch_debug_phases(B->A, B->unit_span, set == PRISMQ_PHASES_PRE ? kIntPre : kIntPost, step, B->st);

@@ -11,6 +11,10 @@ namespace pq {
 
 // Six resident blocks per SM (80 registers) trade a few spilled words for
 // twice the occupancy of the unconstrained 112-register build.
+// R = float: the production step, for the systems whose constraint checks run
+// in FP32 (kCheck64 false) or FP64 (kCheck64 true); R = double: the
+// FP64-everywhere step of an FP64 batch.
+template <class R, bool kCheck64>
 __global__ void __launch_bounds__(128, 6) k_integrate(Arena A, int64_t n_units, int mode) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_units) return;
@@ -19,17 +23,19 @@ __global__ void __launch_bounds__(128, 6) k_integrate(Arena A, int64_t n_units, 
   SysDev* Sp = &A.sys[U.sys];
   const SysDev S = *Sp;
   if (!S.active || S.status != 0) return;
+  if (sizeof(R) == 4 && (S.check64 != 0) != kCheck64) return;
   const long long s = S.step;
   const bool com_step = S.com_interval > 0 && s > 0 && (s % S.com_interval) == 0;
-  UnitState u;
+  UnitStateT<R> u;
   int local[4];
   load_unit(A, U, u, local, S.atom_begin);
   int err = 0;
-  if ((mode & kIntPost) && s > 0) err = phases_post(u, U, S, local, (uint64_t)(s - 1));
+  if ((mode & kIntPost) && s > 0) err = phases_post<R, kCheck64>(u, U, S, local, (uint64_t)(s - 1));
   // On a COM step the pre-phase waits for the per-system COM reduction,
   // which runs in the control kernel.
-  if (!err && (mode & kIntPre) && !com_step) {
-    err = phases_pre(u, U, S, local, (uint64_t)s);
+  const bool pre = (mode & kIntPre) && !com_step;
+  if (!err && pre) {
+    err = phases_pre<R, kCheck64>(u, U, S, local, (uint64_t)s);
     if (!err) check_displacement(A, U, u, Sp);
   }
   if (!err && !unit_finite(u)) err = kStNonfinite;
@@ -37,7 +43,7 @@ __global__ void __launch_bounds__(128, 6) k_integrate(Arena A, int64_t n_units, 
     atomicOr(&Sp->status, err);
     return;
   }
-  store_unit(A, U, u);
+  store_unit(A, U, u, pre);
 }
 
 // Single phase sets for the parity tests; `step` selects the noise.
@@ -53,42 +59,64 @@ __global__ void __launch_bounds__(128) k_debug_phases(Arena A, int64_t n_units, 
   UnitState u;
   int local[4];
   load_unit(A, U, u, local, S.atom_begin);
-  int err = set == kIntPre ? phases_pre(u, U, S, local, (uint64_t)step)
-                           : phases_post(u, U, S, local, (uint64_t)step);
+  int err = set == kIntPre ? phases_pre<float, false>(u, U, S, local, (uint64_t)step)
+                           : phases_post<float, false>(u, U, S, local, (uint64_t)step);
   if (err) atomicOr(&Sp->status, err);
-  store_unit(A, U, u);
+  store_unit(A, U, u, set == kIntPre);
 }
 
-// Per-system energy totals in a fixed reduction order: out[6*s + c] for the
-// five potential planes and the kinetic energy.
+// Per-system totals in a fixed reduction order, out[kEnergyOut*s + c]: the five
+// potential planes, the kinetic energy, then the virial tensor
+// W_ab = Σ_i x_a F_b (row-major, kcal/mol) from the current forces.
 __global__ void __launch_bounds__(256) k_energy_reduce(Arena A, double* out) {
   const int s = blockIdx.x;
   const SysDev S = A.sys[s];
-  __shared__ double red[6][256];
-  double acc[6] = {0, 0, 0, 0, 0, 0};
+  __shared__ double red[kEnergyOut][256];
+  double acc[kEnergyOut];
+  for (int c = 0; c < kEnergyOut; ++c) acc[c] = 0.0;
   if (S.active) {
     for (int i = threadIdx.x; i < S.n_atoms; i += blockDim.x) {
       const int a = S.atom_begin + i;
       for (int c = 0; c < 5; ++c) acc[c] += A.pe[(int64_t)c * A.atom_cap + a];
-      const float4 v = A.vel[a];
-      const double v2 = (double)v.x * v.x + (double)v.y * v.y + (double)v.z * v.z;
-      acc[5] += 0.5 * (double)v.w * v2 / (double)kKcalToAmuA2Ps2;
+      double x[3], v[3], f[3], m;
+      if (A.fp64) {
+        const double4_32a p = A.pos64[a], w = A.vel64[a];
+        x[0] = p.x; x[1] = p.y; x[2] = p.z;
+        v[0] = w.x; v[1] = w.y; v[2] = w.z;
+        m = w.w;
+        for (int d = 0; d < 3; ++d) f[d] = A.f64[(int64_t)d * A.atom_cap + a];
+      } else {
+        const float4 p = A.pos[a], w = A.vel[a];
+        x[0] = p.x; x[1] = p.y; x[2] = p.z;
+        v[0] = w.x; v[1] = w.y; v[2] = w.z;
+        m = w.w;
+        for (int d = 0; d < 3; ++d) f[d] = (double)A.f[(int64_t)d * A.atom_cap + a] * kFixedInvD;
+      }
+      const double v2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+      acc[5] += 0.5 * m * v2 / (double)kKcalToAmuA2Ps2;
+      for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) acc[6 + 3 * r + c] += x[r] * f[c];
     }
   }
-  for (int c = 0; c < 6; ++c) red[c][threadIdx.x] = acc[c];
+  for (int c = 0; c < kEnergyOut; ++c) red[c][threadIdx.x] = acc[c];
   __syncthreads();
   for (int w = 128; w > 0; w >>= 1) {
     if ((int)threadIdx.x < w)
-      for (int c = 0; c < 6; ++c) red[c][threadIdx.x] += red[c][threadIdx.x + w];
+      for (int c = 0; c < kEnergyOut; ++c) red[c][threadIdx.x] += red[c][threadIdx.x + w];
     __syncthreads();
   }
-  if (threadIdx.x < 6) out[6 * s + threadIdx.x] = red[threadIdx.x][0];
+  if (threadIdx.x < kEnergyOut) out[kEnergyOut * s + threadIdx.x] = red[threadIdx.x][0];
 }
 
-void launch_integrate(const Arena& A, int64_t n_units_span, int mode, cudaStream_t st) {
+void launch_integrate(const Arena& A, int64_t n_units_span, int mode, cudaStream_t st, int check64_pass) {
   if (n_units_span <= 0) return;
-  const int64_t blocks = (n_units_span + 127) / 128;
-  k_integrate<<<(unsigned)blocks, 128, 0, st>>>(A, n_units_span, mode);
+  const unsigned blocks = (unsigned)((n_units_span + 127) / 128);
+  if (A.fp64)
+    k_integrate<double, false><<<blocks, 128, 0, st>>>(A, n_units_span, mode);
+  else if (check64_pass)
+    k_integrate<float, true><<<blocks, 128, 0, st>>>(A, n_units_span, mode);
+  else
+    k_integrate<float, false><<<blocks, 128, 0, st>>>(A, n_units_span, mode);
 }
 
 void launch_debug_phases(const Arena& A, int64_t n_units_span, int set, long long step,

@@ -44,13 +44,114 @@ __device__ __forceinline__ int cell_coord(float x, float lo, float inv_edge, int
   return c < 0 ? 0 : (c > n - 1 ? n - 1 : c);
 }
 
+// COM-velocity removal of one system followed by its deferred pre-phase
+// (every com_interval steps; housekeeping.cu:128-183 reduces with FP32
+// atomics).  FP32 systems sum m·v as exact int64 fixed point and m exactly in
+// double; FP64 systems sum in double.  Both reductions use a fixed order, so
+// the result does not depend on scheduling.
+template <class R, bool kCheck64>
+__device__ __noinline__ void com_pre(const Arena& A, SysDev* Sp, long long st, long long (*red_i)[32], double (*red)[32],
+                        double* sh_vcom) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int ab = Sp->atom_begin, na = Sp->n_atoms;
+  long long px = 0, py = 0, pz = 0;
+  double qx = 0.0, qy = 0.0, qz = 0.0, m = 0.0;
+  for (int i = tid; i < na; i += kCtlThreads) {
+    if (sizeof(R) == 4) {
+      const float4 v = A.vel[ab + i];
+      px += f2fixed(v.w * v.x);
+      py += f2fixed(v.w * v.y);
+      pz += f2fixed(v.w * v.z);
+      m += (double)v.w;
+    } else {
+      const double4_32a v = A.vel64[ab + i];
+      qx += v.w * v.x;
+      qy += v.w * v.y;
+      qz += v.w * v.z;
+      m += v.w;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    px += __shfl_xor_sync(0xffffffffu, px, o);
+    py += __shfl_xor_sync(0xffffffffu, py, o);
+    pz += __shfl_xor_sync(0xffffffffu, pz, o);
+    qx += __shfl_xor_sync(0xffffffffu, qx, o);
+    qy += __shfl_xor_sync(0xffffffffu, qy, o);
+    qz += __shfl_xor_sync(0xffffffffu, qz, o);
+    m += __shfl_xor_sync(0xffffffffu, m, o);
+  }
+  if (lane == 0) {
+    red_i[0][warp] = px;
+    red_i[1][warp] = py;
+    red_i[2][warp] = pz;
+    red[0][warp] = qx;
+    red[1][warp] = qy;
+    red[2][warp] = qz;
+    red[3][warp] = m;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    long long IX = 0, IY = 0, IZ = 0;
+    double X = 0.0, Y = 0.0, Z = 0.0, M = 0.0;
+    for (int w = 0; w < 32; ++w) {
+      IX += red_i[0][w];
+      IY += red_i[1][w];
+      IZ += red_i[2][w];
+      X += red[0][w];
+      Y += red[1][w];
+      Z += red[2][w];
+      M += red[3][w];
+    }
+    double c[3] = {0.0, 0.0, 0.0};
+    if (M > 0.0) {
+      if (sizeof(R) == 4) {
+        // the FP32 systems subtract the float COM velocity
+        c[0] = (double)(float)((double)IX * kFixedInvD / M);
+        c[1] = (double)(float)((double)IY * kFixedInvD / M);
+        c[2] = (double)(float)((double)IZ * kFixedInvD / M);
+      } else {
+        c[0] = X / M;
+        c[1] = Y / M;
+        c[2] = Z / M;
+      }
+    }
+    for (int d = 0; d < 3; ++d) {
+      sh_vcom[d] = c[d];
+      Sp->vcom[d] = c[d];
+    }
+  }
+  __syncthreads();
+  const SysDev S = *Sp;
+  for (int t = tid; t < S.n_units; t += kCtlThreads) {
+    const Unit U = A.units[S.unit_begin + t];
+    if (U.nh < 0) continue;
+    UnitStateT<R> u;
+    int local[4];
+    load_unit(A, U, u, local, ab);
+    for (int k = 0; k < u.n; ++k) {
+      u.vx[k] = u.vx[k] - R(sh_vcom[0]);
+      u.vy[k] = u.vy[k] - R(sh_vcom[1]);
+      u.vz[k] = u.vz[k] - R(sh_vcom[2]);
+    }
+    int err = phases_pre<R, kCheck64>(u, U, S, local, (uint64_t)st);
+    if (!err && !unit_finite(u)) err = kStNonfinite;
+    if (err) {
+      atomicOr(&Sp->status, err);
+      continue;
+    }
+    check_displacement(A, U, u, Sp);
+    store_unit(A, U, u, true);
+  }
+  __syncthreads();
+}
+
 __global__ void __launch_bounds__(kCtlThreads) k_control_cells(Arena A, int mode, int nbr_override) {
   extern __shared__ int sm[];  // per-warp sort scratch: 32 * kCellSortCap ints
   __shared__ long long red_i[3][32];
-  __shared__ double red_d[32];
+  __shared__ double red_d[4][32];
   __shared__ float red_f[6][32];
   __shared__ int sh_rb;
-  __shared__ float sh_vcom[3];
+  __shared__ double sh_vcomd[3];
   const int s = blockIdx.x;
   SysDev* Sp = &A.sys[s];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -62,74 +163,12 @@ __global__ void __launch_bounds__(kCtlThreads) k_control_cells(Arena A, int mode
     const long long st = Sp->step;
     const bool com = Sp->com_interval > 0 && st > 0 && (st % Sp->com_interval) == 0;
     if (com) {
-      // Σ m·v as exact int64 fixed point, Σ m exactly in double.
-      long long px = 0, py = 0, pz = 0;
-      double m = 0.0;
-      for (int i = tid; i < na; i += kCtlThreads) {
-        const float4 v = A.vel[ab + i];
-        px += f2fixed(v.w * v.x);
-        py += f2fixed(v.w * v.y);
-        pz += f2fixed(v.w * v.z);
-        m += (double)v.w;
-      }
-      for (int o = 16; o > 0; o >>= 1) {
-        px += __shfl_xor_sync(0xffffffffu, px, o);
-        py += __shfl_xor_sync(0xffffffffu, py, o);
-        pz += __shfl_xor_sync(0xffffffffu, pz, o);
-        m += __shfl_xor_sync(0xffffffffu, m, o);
-      }
-      if (lane == 0) {
-        red_i[0][warp] = px;
-        red_i[1][warp] = py;
-        red_i[2][warp] = pz;
-        red_d[warp] = m;
-      }
-      __syncthreads();
-      if (tid == 0) {
-        long long X = 0, Y = 0, Z = 0;
-        double M = 0.0;
-        for (int w = 0; w < 32; ++w) {
-          X += red_i[0][w];
-          Y += red_i[1][w];
-          Z += red_i[2][w];
-          M += red_d[w];
-        }
-        float cx = 0.0f, cy = 0.0f, cz = 0.0f;
-        if (M > 0.0) {
-          cx = (float)((double)X * kFixedInvD / M);
-          cy = (float)((double)Y * kFixedInvD / M);
-          cz = (float)((double)Z * kFixedInvD / M);
-        }
-        sh_vcom[0] = cx;
-        sh_vcom[1] = cy;
-        sh_vcom[2] = cz;
-        Sp->vcom[0] = cx;
-        Sp->vcom[1] = cy;
-        Sp->vcom[2] = cz;
-      }
-      __syncthreads();
-      const SysDev S = *Sp;
-      for (int t = tid; t < S.n_units; t += kCtlThreads) {
-        const Unit U = A.units[S.unit_begin + t];
-        if (U.nh < 0) continue;
-        UnitState u;
-        int local[4];
-        load_unit(A, U, u, local, ab);
-        for (int k = 0; k < u.n; ++k) {
-          u.vx[k] = u.vx[k] - sh_vcom[0];
-          u.vy[k] = u.vy[k] - sh_vcom[1];
-          u.vz[k] = u.vz[k] - sh_vcom[2];
-        }
-        int err = phases_pre(u, U, S, local, (uint64_t)st);
-        if (!err && !unit_finite(u)) err = kStNonfinite;
-        if (err) {
-          atomicOr(&Sp->status, err);
-          continue;
-        }
-        check_displacement(A, U, u, Sp);
-        store_unit(A, U, u);
-      }
-      __syncthreads();
+      if (A.fp64)
+        com_pre<double, false>(A, Sp, st, red_i, red_d, sh_vcomd);
+      else if (Sp->check64)
+        com_pre<float, true>(A, Sp, st, red_i, red_d, sh_vcomd);
+      else
+        com_pre<float, false>(A, Sp, st, red_i, red_d, sh_vcomd);
     }
   }
 

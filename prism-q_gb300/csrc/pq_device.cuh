@@ -86,6 +86,11 @@ struct SysDev {
   int pad1;
   double vcom[3];
   long long n_rebuilds;  // list builds so far (statistics)
+  // constraint convergence (reference: SHAKE 1e-4 on |r^2-L^2|/L^2, RATTLE 1e-5)
+  float shake_tol, rattle_tol;
+  int check64;  // 1: constraint residuals and multipliers evaluated in FP64
+  int pad2;
+  double c1d;   // exp(-γ·dt/2) in double (FP64 batches)
 };
 
 // Per-atom incidence into bonded term arrays (reference: atom_bond_list etc.,
@@ -133,6 +138,14 @@ struct Arena {
   int* work_ctl = nullptr;
   // systems
   SysDev* sys = nullptr;
+  // FP64 batches only (null otherwise): the state and forces of the
+  // FP64-everywhere run; pos/vel above then hold its FP32 rounding, which the
+  // cell and neighbour-row kernels read.
+  int fp64 = 0;
+  double4_32a* pos64 = nullptr;  // x y z q
+  double4_32a* vel64 = nullptr;  // vx vy vz mass
+  double* f64 = nullptr;     // 3 planes of atom_cap
+  double2* lj64 = nullptr;   // sigma/2, sqrt(eps) in double
 };
 
 // K2 modes
@@ -154,9 +167,12 @@ void launch_force(const Arena& A, int64_t n_atoms_span, bool energy, cudaStream_
                   bool only_rebuilt = false, int variant = 0);
 int force_variant_count();
 void force_variant_shape(int variant, int* block, int* min_blocks);
-void launch_integrate(const Arena& A, int64_t n_units_span, int mode, cudaStream_t st);
+// check64_pass: 0 = systems with FP32 constraint checks, 1 = systems with FP64
+// checks (FP32 batches launch one pass per kind present); FP64 batches ignore it.
+void launch_integrate(const Arena& A, int64_t n_units_span, int mode, cudaStream_t st, int check64_pass = 0);
 void launch_debug_phases(const Arena& A, int64_t n_units_span, int set, long long step,
                          cudaStream_t st);
-void launch_energy_reduce(const Arena& A, int n_sys, double* out6, cudaStream_t st);
+constexpr int kEnergyOut = 15;  // per system: 5 potential planes, kinetic, 3x3 virial
+void launch_energy_reduce(const Arena& A, int n_sys, double* out, cudaStream_t st);
 
 }  // namespace pq

@@ -248,6 +248,10 @@ prismq_status prismq_server_submit(prismq_server* s, const prismq_job* job, int6
     pq::set_last_error("n_steps must be >= 1");
     return PRISMQ_E_INVALID;
   }
+  if (job->params.precision != PRISMQ_PRECISION_FP32) {
+    pq::set_last_error("the server runs FP32 (production) jobs");
+    return PRISMQ_E_INVALID;
+  }
   pq::PreparedSystem* prep = nullptr;
   const prismq_status rc = pq::prepare_system(job->topology, &job->params, &prep);
   if (rc != PRISMQ_OK) return rc;

@@ -38,7 +38,8 @@ def test_server_structs_match_the_header(pq):
     # sizes of the C structs on LP64 (x86-64 and aarch64): the ctypes mirrors
     # must agree or every field after the first mismatch is misread
     assert ctypes.sizeof(pq.ServerConfigStruct) == 16
-    assert ctypes.sizeof(pq.JobStruct) == 80
+    assert ctypes.sizeof(pq.JobStruct) == 96
+    assert ctypes.sizeof(pq.ParamsStruct) == 56
     assert ctypes.sizeof(pq.JobResultStruct) == 216
     assert ctypes.sizeof(pq.ServerStatsStruct) == 96
 
