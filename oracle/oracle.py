@@ -61,6 +61,11 @@ def lib() -> ctypes.CDLL:
         L.orc_forces_ref_f32.argtypes = [P, P, P, ctypes.c_int]
         L.orc_forces_f64.argtypes = [P, P, P, ctypes.c_int]
         L.orc_forces_f64_rule.argtypes = [P, P, P, ctypes.c_int, ctypes.c_int]
+        L.orc_rattle_all.argtypes = [P]
+        L.orc_shake_all.argtypes = [P, P]
+        L.orc_kick_all.argtypes = [P, P]
+        L.orc_clamp_all.argtypes = [P]
+        L.orc_term_forces.argtypes = [P, P, P, P]
         L.orc_phases.argtypes = [P, ctypes.c_int, P, ctypes.c_longlong]
         L.orc_com_remove.argtypes = [P]
         L.orc_run.argtypes = [P, ctypes.c_long, ctypes.c_int]
@@ -182,6 +187,28 @@ class OracleSystem:
         e = np.zeros(5, dtype=np.float64)
         lib().orc_forces_f64_rule(self.h, _ptr(f), _ptr(e), threads, 1 if incl64 else 0)
         return f, e
+
+    # single pieces on the current state (pins against the reference's own functions)
+    def rattle_all(self) -> int:
+        return lib().orc_rattle_all(self.h)
+
+    def shake_all(self, x_start) -> int:
+        xs = np.ascontiguousarray(x_start, dtype=np.float32).reshape(-1)
+        return lib().orc_shake_all(self.h, _ptr(xs))
+
+    def kick_all(self, f) -> None:
+        fa = np.ascontiguousarray(f, dtype=np.float32).reshape(-1)
+        lib().orc_kick_all(self.h, _ptr(fa))
+
+    def clamp_all(self) -> None:
+        lib().orc_clamp_all(self.h)
+
+    def term_forces(self, nb: int, na: int, nd: int):
+        fb = np.zeros((nb, 2, 3), np.float32)
+        fa = np.zeros((na, 3, 3), np.float32)
+        fd = np.zeros((nd, 4, 3), np.float32)
+        lib().orc_term_forces(self.h, _ptr(fb), _ptr(fa), _ptr(fd))
+        return fb, fa, fd
 
     def phases(self, which: int, f_fixed: np.ndarray, step: int) -> int:
         ff = np.ascontiguousarray(f_fixed, dtype=np.int64).reshape(-1)

@@ -1125,6 +1125,44 @@ static int phases_post_f(orc_sys* s, const float* f, long long step) {
   return all_rattle(s);
 }
 
+/* Single integrator pieces and per-term forces on the current state.  These
+ * are the units the pins against the reference's own device functions
+ * compare (tests/test_reference_kernels.py). */
+int orc_rattle_all(orc_sys* s) { return all_rattle(s); }
+
+int orc_shake_all(orc_sys* s, const float* xs) {
+  int err = 0;
+  for (int c = 0; c < s->ncl; ++c) err |= shake_cluster(s, &s->cl[c], xs);
+  return err;
+}
+
+void orc_kick_all(orc_sys* s, const float* f) {
+  for (int a = 0; a < s->n; ++a) kick_atom(s, a, f);
+}
+
+void orc_clamp_all(orc_sys* s) {
+  for (int a = 0; a < s->n; ++a) clamp_atom(s, a);
+}
+
+/* bonds -> fb[nb][2][3], angles -> fa[na][3][3], torsion terms -> fd[nd][4][3] */
+void orc_term_forces(const orc_sys* s, float* fb, float* fa, float* fd) {
+  for (int t = 0; t < s->nb; ++t) {
+    float* o = fb + 6 * (size_t)t;
+    for (int k = 0; k < 6; ++k) o[k] = 0.0f;
+    bond_f32(s->x, &s->bonds[t], o, o + 3, NULL);
+  }
+  for (int t = 0; t < s->na; ++t) {
+    float* o = fa + 9 * (size_t)t;
+    for (int k = 0; k < 9; ++k) o[k] = 0.0f;
+    angle_f32(s->x, &s->angles[t], o, o + 3, o + 6, NULL);
+  }
+  for (int t = 0; t < s->nd; ++t) {
+    float* o = fd + 12 * (size_t)t;
+    for (int k = 0; k < 12; ++k) o[k] = 0.0f;
+    dihedral_f32(s->x, &s->dihs[t], o, o + 3, o + 6, o + 9, NULL);
+  }
+}
+
 int orc_phases(orc_sys* s, int set, const int64_t* f_fixed, long long step) {
   const int n = s->n;
   float* f = (float*)malloc(sizeof(float) * 3 * (size_t)n);

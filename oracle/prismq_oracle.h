@@ -70,6 +70,11 @@ int orc_forces_ref_f32(orc_sys* s, float* f, double* e5, int threads);
  * arithmetic in double. */
 int orc_forces_f64(orc_sys* s, double* f, double* e5, int threads);
 int orc_forces_f64_rule(orc_sys* s, double* f, double* e5, int threads, int incl64);
+int orc_rattle_all(orc_sys* s);
+int orc_shake_all(orc_sys* s, const float* xs);
+void orc_kick_all(orc_sys* s, const float* f);
+void orc_clamp_all(orc_sys* s);
+void orc_term_forces(const orc_sys* s, float* fb, float* fa, float* fd);
 
 /* Integrator phase sets on the current state with forces given as int64
  * fixed point (2^-32 kcal/mol/Å).  set 1 = OU½, RATTLE, KICK½, RATTLE, DRIFT,
