@@ -387,8 +387,8 @@ __global__ void __launch_bounds__(kCtlThreads) k_control_cells(Arena A, int mode
 }
 
 // Persistent row builder: resident CTAs of eight warps pull 8-atom groups of
-// rebuilding systems from the work list; warp w builds the row of atom
-// 8*group + w and writes each kept neighbour straight into the tiled layout.
+// rebuilding systems from the work list and write each kept neighbour
+// straight into the tiled layout.
 constexpr int kNbrThreads = 256;
 
 __device__ __forceinline__ void build_row(const Arena& A, int a, int exclude_exc, int lane, int* count_out) {
@@ -498,17 +498,202 @@ __device__ __forceinline__ void build_row(const Arena& A, int a, int exclude_exc
   *count_out = count;
 }
 
-// Warps walk the queued atoms round-robin (no shared counter, no atomics); the
-// force kernel that follows in the same stream clears the queue.
-__global__ void __launch_bounds__(kNbrThreads) k_nbr_build(Arena A, int64_t n_span, int exclude_exc) {
-  const int lane = threadIdx.x & 31;
-  const int64_t gw = (int64_t)blockIdx.x * (kNbrThreads / 32) + (threadIdx.x >> 5);
+// Per-warp data of the group being built: the atoms' exclusion data and the
+// candidate runs (one per cell row of the union stencil, in (z, y) order).
+constexpr int kMaxRuns = 96;
+struct GroupShared {
+  unsigned long long mask[8];
+  int2 far[8];
+  int run_b[kMaxRuns];        // first sorted-atom index of the run
+  int run_off[kMaxRuns + 1];  // exclusive prefix of run lengths
+};
+
+// Test one candidate against every atom of the group and append the kept ones
+// to the atoms' rows (ballot compaction keeps candidate order).
+__device__ __forceinline__ void group_test(const Arena& A, const GroupShared& sh, const float4 (&P)[8], int n_act,
+                                           int a0, int g, bool valid, int j, float4 pj, float r2max,
+                                           int exclude_exc, unsigned lt, int (&cnt)[8], unsigned& ovf) {
+  int* const rows = A.nbr + (int64_t)g * kNbrCap * 8;  // tiled rows of the group's 8 atoms
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    if (i >= n_act) break;
+    const int ai = a0 + i;
+    bool keep = valid && j != ai;
+    if (keep) keep = !(r2_nofma(pj.x - P[i].x, pj.y - P[i].y, pj.z - P[i].z) > r2max);
+    if (keep) {
+      const int d = j - ai;
+      if (d >= -32 && d < 32) {
+        if ((sh.mask[i] >> (d + 32)) & 1ull) keep = false;
+      } else {
+        const int2 far = sh.far[i];
+        for (int q = 0; q < far.y; ++q) {
+          const int ent = A.far_list[far.x + q];
+          if ((ent & 0x3fffffff) == j && (exclude_exc || !(ent & 0x40000000))) {
+            keep = false;
+            break;
+          }
+        }
+      }
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, keep);
+    const int add = __popc(bal);
+    if (cnt[i] + add > kNbrCap) {
+      ovf |= 1u << i;
+    } else {
+      if (keep) {
+        const int k = cnt[i] + __popc(bal & lt);  // same slot as nbr_index(ai, k)
+        rows[(k & ~3) * 8 + (i << 2) + (k & 3)] = j;
+      }
+      cnt[i] += add;
+    }
+  }
+}
+
+// Complete-mode rows of one 8-atom group, built together: the warp lists the
+// cell-row runs of the union of the group's stencils (the rows and x-runs
+// within r_list of the group's bounding box), packs their candidates into
+// one stream of full 32-lane iterations, and tests every candidate against
+// each atom of the group.  Each atom's row comes out identical to a scan of
+// its own stencil: the union visits a superset of that atom's rows and
+// x-runs in the same (z, y, x, atom) order, and a candidate is kept by the
+// same r^2 and exclusion tests.
+__device__ __forceinline__ void build_group(const Arena& A, int64_t g, int exclude_exc, int lane,
+                                            GroupShared& sh) {
+  const int a0 = (int)(g * 8);
+  const int s = A.atom_sys[a0];
+  SysDev* Sp = s >= 0 ? &A.sys[s] : nullptr;
+  if (!Sp || !Sp->active || !Sp->rebuilding || Sp->status != 0) return;
+  const int ab = Sp->atom_begin;
+  const int n_act = min(8, ab + Sp->n_atoms - a0);
+  const int dims[3] = {Sp->g_dims[0], Sp->g_dims[1], Sp->g_dims[2]};
+  const float r2max = Sp->rlist2;
+  const int* start = A.cell_start + Sp->cell_begin;
+  float4 P[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) P[i] = A.pos[a0 + min(i, n_act - 1)];
+  if (lane < n_act) {
+    sh.mask[lane] = exclude_exc ? A.mask_all[a0 + lane] : A.mask_ref[a0 + lane];
+    sh.far[lane] = A.far[a0 + lane];
+  }
+  float bl[3] = {P[0].x, P[0].y, P[0].z}, bh[3] = {P[0].x, P[0].y, P[0].z};
+#pragma unroll
+  for (int i = 1; i < 8; ++i) {
+    bl[0] = fminf(bl[0], P[i].x);
+    bl[1] = fminf(bl[1], P[i].y);
+    bl[2] = fminf(bl[2], P[i].z);
+    bh[0] = fmaxf(bh[0], P[i].x);
+    bh[1] = fmaxf(bh[1], P[i].y);
+    bh[2] = fmaxf(bh[2], P[i].z);
+  }
+  const float lox = Sp->g_lo[0], loy = Sp->g_lo[1], loz = Sp->g_lo[2];
+  const float ivx = Sp->g_inv_edge[0], ivy = Sp->g_inv_edge[1], ivz = Sp->g_inv_edge[2];
+  const float ey = 1.0f / ivy, ez = 1.0f / ivz;
+  const float rl = sqrtf(r2max) + 1.0e-3f;
+  const int z0 = max((int)((bl[2] - rl - loz) * ivz), 0), z1 = min((int)((bh[2] + rl - loz) * ivz), dims[2] - 1);
+  const int y0 = max((int)((bl[1] - rl - loy) * ivy), 0), y1 = min((int)((bh[1] + rl - loy) * ivy), dims[1] - 1);
+  const int ny = y1 - y0 + 1;
+  const int n_rows = (z1 - z0 + 1) * ny;
+  if (n_rows > kMaxRuns) {
+    // a group that spans two distant chains: build its rows atom by atom
+    for (int i = 0; i < n_act; ++i) {
+      int count = -1;
+      build_row(A, a0 + i, exclude_exc, lane, &count);
+    }
+    return;
+  }
+  // ---- the runs of candidates, one per (z, y) cell row, in scan order ----
+  int total = 0;
+  for (int r0 = 0; r0 < n_rows; r0 += 32) {
+    const int r = r0 + lane;
+    int b = 0, len = 0;
+    if (r < n_rows) {
+      const int z = z0 + r / ny, y = y0 + r % ny;
+      const float sz = fmaxf(0.0f, fmaxf((loz + (float)z * ez) - bh[2], bl[2] - (loz + (float)(z + 1) * ez)));
+      const float sy = fmaxf(0.0f, fmaxf((loy + (float)y * ey) - bh[1], bl[1] - (loy + (float)(y + 1) * ey)));
+      const float mz = fmaxf(sz - 1.0e-3f, 0.0f), my = fmaxf(sy - 1.0e-3f, 0.0f);
+      const float d2 = my * my + mz * mz;
+      if (!(d2 > r2max)) {
+        const float xr = sqrtf(r2max - d2) + 1.0e-3f;
+        const int x0 = max((int)((bl[0] - xr - lox) * ivx), 0);
+        const int x1 = min((int)((bh[0] + xr - lox) * ivx), dims[0] - 1);
+        if (x0 <= x1) {
+          const int rowc = y * dims[0] + z * dims[0] * dims[1];
+          b = start[rowc + x0];
+          len = start[rowc + x1 + 1] - b;
+        }
+      }
+    }
+    int incl = len;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    if (r < n_rows) {
+      sh.run_b[r] = b;
+      sh.run_off[r] = total + incl - len;
+    }
+    total += __shfl_sync(0xffffffffu, incl, 31);
+  }
+  if (lane == 0) sh.run_off[n_rows] = total;
+  __syncwarp();
+  // ---- the packed candidate stream, loads of the next chunk in flight ----
+  auto locate = [&](int c) -> int {  // sorted-atom index of candidate c (c < total)
+    int lo = 0, hi = n_rows - 1;  // last run with run_off <= c
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (sh.run_off[mid] <= c) lo = mid; else hi = mid - 1;
+    }
+    return sh.run_b[lo] + (c - sh.run_off[lo]);
+  };
+  int cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  unsigned ovf = 0u;
+  const unsigned lt = (1u << lane) - 1u;
+  int c = lane;
+  int j = c < total ? A.cell_atoms[ab + locate(c)] : -1;
+  for (int c0 = 0; c0 < total; c0 += 32) {
+    const bool valid = c < total;
+    const float4 pj = valid ? A.pos[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const int cn = c + 32;
+    const int jn = cn < total ? A.cell_atoms[ab + locate(cn)] : -1;
+    group_test(A, sh, P, n_act, a0, (int)g, valid, j, pj, r2max, exclude_exc, lt, cnt, ovf);
+    c = cn;
+    j = jn;
+  }
+  if (ovf) {
+    if (lane == 0) atomicOr(&Sp->status, kStNbrOverflow);
+    return;
+  }
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+    if (lane == i && i < n_act) {
+      A.nnbr[a0 + i] = cnt[i];
+      A.xref[a0 + i] = P[i];
+    }
+  __syncwarp();
+}
+
+// Warps walk the queued 8-atom groups round-robin (no shared counter, no
+// atomics); the force kernel that follows in the same stream clears the
+// queue.  Complete lists are built a group at a time; REF27 lists (parity
+// only) atom by atom with the reference's own 27-cell stencil.
+__global__ void __launch_bounds__(kNbrThreads, 3) k_nbr_build(Arena A, int64_t n_span, int exclude_exc) {
+  __shared__ GroupShared sh[kNbrThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t gw = (int64_t)blockIdx.x * (kNbrThreads / 32) + warp;
   const int64_t n_warps = (int64_t)gridDim.x * (kNbrThreads / 32);
-  const int64_t n_rows = (int64_t)A.work_ctl[0] * 8;
-  for (int64_t v = gw; v < n_rows; v += n_warps) {
-    const int64_t a64 = (int64_t)A.work[v >> 3] * 8 + (v & 7);
-    int count = -1;
-    if (a64 < n_span) build_row(A, (int)a64, exclude_exc, lane, &count);
+  const int64_t n_groups = A.work_ctl[0];
+  for (int64_t v = gw; v < n_groups; v += n_warps) {
+    const int64_t g = A.work[v];
+    if (g * 8 >= n_span) continue;
+    const int s = A.atom_sys[g * 8];
+    if (s >= 0 && A.sys[s].nbr_mode == 1) {
+      for (int i = 0; i < 8; ++i) {
+        int count = -1;
+        if (g * 8 + i < n_span) build_row(A, (int)(g * 8 + i), exclude_exc, lane, &count);
+      }
+    } else {
+      build_group(A, g, exclude_exc, lane, sh[warp]);
+    }
   }
 }
 
