@@ -525,7 +525,7 @@ struct prismq_batch {
     if (gexec) cudaGraphExecDestroy(gexec);
     void* ptrs[] = {A.pos, A.vel, A.lj, A.xref, A.f, A.pe, A.atom_sys, A.mask_all, A.mask_ref, A.far,
                     A.far_list, A.inc, A.inc_list, A.ex_idx, A.ex_partner, A.ex_par, A.bonds, A.angles,
-                    A.dihs, A.units, A.nbr, A.nnbr, A.cell_start, A.cell_atoms, A.atom_cell, A.work, A.work_ctl, A.sys,
+                    A.dihs, A.units, A.noise, A.nbr, A.nnbr, A.cell_start, A.cell_atoms, A.atom_cell, A.work, A.work_ctl, A.sys,
                     A.pos64, A.vel64, A.f64, A.lj64, d_energy, d_stage, d_stage2, d_stage64};
     for (void* p : ptrs)
       if (p) cudaFree(p);
@@ -561,11 +561,12 @@ struct prismq_batch {
   // batches run one pass per constraint-check precision present.  Returns the
   // number of kernels launched.
   int integrate(int mode) {
+    launch_noise(A, atom_span, mode, st);
     if (A.fp64) {
       launch_integrate(A, unit_span, mode, st, 0);
-      return 1;
+      return 2;
     }
-    int k = 0;
+    int k = 1;
     if (n_check32 > 0 || n_check64 == 0) {
       launch_integrate(A, unit_span, mode, st, 0);
       ++k;
@@ -576,7 +577,9 @@ struct prismq_batch {
     }
     return k;
   }
-  int integrate_passes() const { return A.fp64 ? 1 : (n_check32 > 0 || n_check64 == 0 ? 1 : 0) + (n_check64 > 0 ? 1 : 0); }
+  int integrate_passes() const {
+    return 1 + (A.fp64 ? 1 : (n_check32 > 0 || n_check64 == 0 ? 1 : 0) + (n_check64 > 0 ? 1 : 0));
+  }
 
   void enqueue_step_body() {
     launch_control_cells(A, sys_span, kCtlStep, -1, st);
@@ -805,6 +808,7 @@ prismq_status batch_alloc(prismq_batch* B, int64_t atom_cap, int sys_cap, int64_
   PQ_ALLOC(A.angles, A.angle_cap);
   PQ_ALLOC(A.dihs, A.dih_cap);
   PQ_ALLOC(A.units, A.unit_cap);
+  PQ_ALLOC(A.noise, 2 * atom_cap);
   PQ_ALLOC(A.nbr, (atom_cap / 32) * (int64_t)kNbrCap * 32);
   PQ_ALLOC(A.nnbr, atom_cap);
   PQ_ALLOC(A.cell_start, A.cell_cap);

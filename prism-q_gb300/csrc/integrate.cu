@@ -9,13 +9,14 @@
 
 namespace pq {
 
-// Six resident blocks per SM (80 registers) trade a few spilled words for
-// twice the occupancy of the unconstrained 112-register build.
+// One thread per constraint unit.  The OU normals arrive drawn (k_noise), and
+// eight resident blocks per SM (64 registers) trade a few spilled words for
+// 1.4x the occupancy of the unconstrained 91-register build.
 // R = float: the production step, for the systems whose constraint checks run
 // in FP32 (kCheck64 false) or FP64 (kCheck64 true); R = double: the
 // FP64-everywhere step of an FP64 batch.
 template <class R, bool kCheck64>
-__global__ void __launch_bounds__(128, 6) k_integrate(Arena A, int64_t n_units, int mode) {
+__global__ void __launch_bounds__(128, 8) k_integrate(Arena A, int64_t n_units, int mode) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_units) return;
   const Unit U = A.units[t];
@@ -30,12 +31,12 @@ __global__ void __launch_bounds__(128, 6) k_integrate(Arena A, int64_t n_units, 
   int local[4];
   load_unit(A, U, u, local, S.atom_begin);
   int err = 0;
-  if ((mode & kIntPost) && s > 0) err = phases_post<R, kCheck64>(u, U, S, local, (uint64_t)(s - 1));
+  if ((mode & kIntPost) && s > 0) err = phases_post<R, kCheck64, true>(u, U, S, local, (uint64_t)(s - 1), A.noise);
   // On a COM step the pre-phase waits for the per-system COM reduction,
   // which runs in the control kernel.
   const bool pre = (mode & kIntPre) && !com_step;
   if (!err && pre) {
-    err = phases_pre<R, kCheck64>(u, U, S, local, (uint64_t)s);
+    err = phases_pre<R, kCheck64, true>(u, U, S, local, (uint64_t)s, A.noise + A.atom_cap);
     if (!err) check_displacement(A, U, u, Sp);
   }
   if (!err && !unit_finite(u)) err = kStNonfinite;
@@ -44,6 +45,36 @@ __global__ void __launch_bounds__(128, 6) k_integrate(Arena A, int64_t n_units, 
     return;
   }
   store_unit(A, U, u, pre);
+}
+
+// The OU normals of the next integrate launch, one thread per atom.  Drawing
+// them here, with every atom in flight at once, takes the Philox rounds and
+// the Box–Muller series out of the integrator's per-unit dependency chains;
+// the values are the ones normal3 gives there, bit for bit.
+__global__ void __launch_bounds__(256) k_noise(Arena A, int64_t n_atoms, int mode) {
+  const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= n_atoms) return;
+  const int sid = A.atom_sys[a];
+  if (sid < 0) return;
+  const SysDev& S = A.sys[sid];
+  if (!S.active || S.status != 0 || S.gamma == 0.0f) return;
+  const long long s = S.step;
+  const uint32_t local = (uint32_t)(a - S.atom_begin);
+  float z0, z1, z2;
+  if ((mode & kIntPost) && s > 0) {
+    normal3(S.seed, S.stream, local, (uint64_t)(s - 1), kPurposeOuNp1, &z0, &z1, &z2);
+    A.noise[a] = make_float4(z0, z1, z2, 0.0f);
+  }
+  const bool com_step = S.com_interval > 0 && s > 0 && (s % S.com_interval) == 0;
+  if ((mode & kIntPre) && !com_step) {
+    normal3(S.seed, S.stream, local, (uint64_t)s, kPurposeOuN, &z0, &z1, &z2);
+    A.noise[A.atom_cap + a] = make_float4(z0, z1, z2, 0.0f);
+  }
+}
+
+void launch_noise(const Arena& A, int64_t n_atoms_span, int mode, cudaStream_t st) {
+  if (n_atoms_span <= 0) return;
+  k_noise<<<(unsigned)((n_atoms_span + 255) / 256), 256, 0, st>>>(A, n_atoms_span, mode);
 }
 
 // Single phase sets for the parity tests; `step` selects the noise.

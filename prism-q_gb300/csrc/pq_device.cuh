@@ -127,6 +127,9 @@ struct Arena {
   DihT* dihs = nullptr;
   // constraint units
   Unit* units = nullptr;
+  // OU normals drawn ahead of the integrate launch, per atom: [0, atom_cap)
+  // for post(s-1), [atom_cap, 2 atom_cap) for pre(s)
+  float4* noise = nullptr;
   // lists
   int* nbr = nullptr;   // tiled rows, see nbr_index()
   int* nnbr = nullptr;  // row lengths
@@ -170,6 +173,8 @@ void force_variant_shape(int variant, int* block, int* min_blocks);
 // check64_pass: 0 = systems with FP32 constraint checks, 1 = systems with FP64
 // checks (FP32 batches launch one pass per kind present); FP64 batches ignore it.
 void launch_integrate(const Arena& A, int64_t n_units_span, int mode, cudaStream_t st, int check64_pass = 0);
+// Draw the OU normals the next integrate launch of `mode` uses.
+void launch_noise(const Arena& A, int64_t n_atoms_span, int mode, cudaStream_t st);
 void launch_debug_phases(const Arena& A, int64_t n_units_span, int set, long long step,
                          cudaStream_t st);
 constexpr int kEnergyOut = 15;  // per system: 5 potential planes, kinetic, 3x3 virial

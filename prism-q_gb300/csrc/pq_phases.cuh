@@ -68,16 +68,26 @@ struct UnitStateT {
 };
 using UnitState = UnitStateT<float>;
 
-template <class R>
-__device__ __forceinline__ void ou_half(UnitStateT<R>& u, const SysDev& S, const int* atom_local, uint64_t step,
-                                        uint32_t purpose) {
+// OU half step.  With kDrawn the normals come from `znoise` (indexed by global
+// atom, drawn ahead by k_noise with the same normal3); otherwise they are
+// drawn here.
+template <class R, bool kDrawn>
+__device__ __forceinline__ void ou_half(UnitStateT<R>& u, const Unit& U, const SysDev& S, const int* atom_local,
+                                        uint64_t step, uint32_t purpose, const float4* znoise) {
   if (S.gamma == 0.0f) return;
   const R c1 = PhaseConst<R>::c1(S);
   PQ_UNROLL for (int k = 0; k < 4; ++k) {
     if (k >= u.n) break;
     const R c2 = sqrt_r((R(1.0f) - c1 * c1) * PhaseConst<R>::kcal() * PhaseConst<R>::kb() * R(S.temperature) / u.m[k]);
     float z0, z1, z2;
-    normal3(S.seed, S.stream, (uint32_t)atom_local[k], step, purpose, &z0, &z1, &z2);
+    if constexpr (kDrawn) {
+      const float4 z = znoise[U.a[k]];
+      z0 = z.x;
+      z1 = z.y;
+      z2 = z.z;
+    } else {
+      normal3(S.seed, S.stream, (uint32_t)atom_local[k], step, purpose, &z0, &z1, &z2);
+    }
     u.vx[k] = c1 * u.vx[k] + c2 * R(z0);
     u.vy[k] = c1 * u.vy[k] + c2 * R(z1);
     u.vz[k] = c1 * u.vz[k] + c2 * R(z2);
@@ -295,12 +305,12 @@ __device__ __forceinline__ void store_unit(const Arena& A, const Unit& U, const 
 
 // Post-force phases of step s: KICK_NP1 → RATTLE_BEFORE_OU_NP1 → OU_HALF_NP1,
 // then the post-step velocity clamp and final RATTLE (fused_engine.rs:17498-17800).
-template <class R, bool kCheck64>
+template <class R, bool kCheck64, bool kDrawn = false>
 __device__ __forceinline__ int phases_post(UnitStateT<R>& u, const Unit& U, const SysDev& S, const int* local,
-                                           uint64_t s) {
+                                           uint64_t s, const float4* znoise = nullptr) {
   half_kick(u, S);
   if (!rattle<R, kCheck64>(u, U, S)) return kStRattle;
-  ou_half(u, S, local, s, kPurposeOuNp1);
+  ou_half<R, kDrawn>(u, U, S, local, s, kPurposeOuNp1, znoise);
   velocity_clamp(u, S);
   if (!rattle<R, kCheck64>(u, U, S)) return kStRattle;
   return 0;
@@ -308,10 +318,10 @@ __device__ __forceinline__ int phases_post(UnitStateT<R>& u, const Unit& U, cons
 
 // Pre-force phases of step s: OU_HALF_N → RATTLE_AFTER_OU_N → KICK_N →
 // RATTLE_PRE_DRIFT → DRIFT_SAVE_XN → SHAKE_POSITION.
-template <class R, bool kCheck64>
+template <class R, bool kCheck64, bool kDrawn = false>
 __device__ __forceinline__ int phases_pre(UnitStateT<R>& u, const Unit& U, const SysDev& S, const int* local,
-                                          uint64_t s) {
-  ou_half(u, S, local, s, kPurposeOuN);
+                                          uint64_t s, const float4* znoise = nullptr) {
+  ou_half<R, kDrawn>(u, U, S, local, s, kPurposeOuN, znoise);
   if (!rattle<R, kCheck64>(u, U, S)) return kStRattle;
   half_kick(u, S);
   if (!rattle<R, kCheck64>(u, U, S)) return kStRattle;
