@@ -122,6 +122,10 @@ struct Lowered {
   std::vector<AngleT> angles;
   std::vector<DihT> dihs;
   std::vector<Unit> units;
+  std::vector<ExcT> excs;       // exception pairs, each once
+  std::vector<int2> grp;        // per 32-atom group: {begin, count} into grp_refs (local)
+  std::vector<int> grp_refs;    // kind << 29 | local term index
+  int max_group_slots = 0;      // bonded + exception incidences of the fullest group
   std::vector<float> charges, masses;
   float ref_origin[3] = {0, 0, 0};
   int ref_dims[3] = {1, 1, 1};
@@ -168,7 +172,7 @@ prismq_status lower_topology(const prismq_topology* T, Lowered* L) {
     const prismq_bond& b = T->bonds[t];
     if (!in_range(b.i) || !in_range(b.j) || b.i == b.j)
       return fail(PRISMQ_E_INVALID, "bond " + std::to_string(t) + " has invalid atoms");
-    L->bonds.push_back({b.i, b.j, b.r0, b.k});
+    L->bonds.push_back({b.i, b.j, b.r0, b.k, (int)ib[b.i].size() | ((int)ib[b.j].size() << 16)});
     ib[b.i].push_back(t * 4 + 0);
     ib[b.j].push_back(t * 4 + 1);
   }
@@ -176,7 +180,10 @@ prismq_status lower_topology(const prismq_topology* T, Lowered* L) {
     const prismq_angle& g = T->angles[t];
     if (!in_range(g.i) || !in_range(g.j) || !in_range(g.k) || g.i == g.j || g.j == g.k || g.i == g.k)
       return fail(PRISMQ_E_INVALID, "angle " + std::to_string(t) + " has invalid atoms");
-    L->angles.push_back({g.i, g.j, g.k, g.theta0, g.force_k});
+    // positions past 1023 overflow the packing; such atoms are rejected below (> 255)
+    L->angles.push_back({g.i, g.j, g.k, g.theta0, g.force_k,
+                         ((int)ia[g.i].size() & 1023) | (((int)ia[g.j].size() & 1023) << 10) |
+                             (((int)ia[g.k].size() & 1023) << 20)});
     ia[g.i].push_back(t * 4 + 0);
     ia[g.j].push_back(t * 4 + 1);
     ia[g.k].push_back(t * 4 + 2);
@@ -185,7 +192,9 @@ prismq_status lower_topology(const prismq_topology* T, Lowered* L) {
     const prismq_dihedral& d = T->dihedrals[t];
     if (!in_range(d.i) || !in_range(d.j) || !in_range(d.k) || !in_range(d.l))
       return fail(PRISMQ_E_INVALID, "dihedral " + std::to_string(t) + " has invalid atoms");
-    L->dihs.push_back({d.i, d.j, d.k, d.l, d.periodicity, d.phase, d.force_k});
+    L->dihs.push_back({d.i, d.j, d.k, d.l, d.periodicity, d.phase, d.force_k,
+                       ((int)id[d.i].size() & 255) | (((int)id[d.j].size() & 255) << 8) |
+                           (((int)id[d.k].size() & 255) << 16) | (((int)id[d.l].size() & 255) << 24)});
     id[d.i].push_back(t * 4 + 0);
     id[d.j].push_back(t * 4 + 1);
     id[d.k].push_back(t * 4 + 2);
@@ -222,11 +231,69 @@ prismq_status lower_topology(const prismq_topology* T, Lowered* L) {
   }
   L->ex_idx.resize(n);
   for (int a = 0; a < n; ++a) {
+    if (exc[a].size() > 65535) return fail(PRISMQ_E_INVALID, "too many exceptions on atom " + std::to_string(a));
     L->ex_idx[a] = make_int2((int)L->ex_partner.size(), (int)exc[a].size());
     for (auto& kv : exc[a]) {
       L->ex_partner.push_back(kv.first);
       L->ex_par.push_back(kv.second);
     }
+  }
+  // each exception pair once, with its rank in both members' ascending lists
+  for (int a = 0; a < n; ++a) {
+    int ra = 0;
+    for (auto& kv : exc[a]) {
+      const int j = kv.first;
+      if (j > a) {
+        const int rj = (int)std::distance(exc[j].begin(), exc[j].find(a));
+        L->excs.push_back({a, j, kv.second.x, kv.second.y, kv.second.z, ra | (rj << 16)});
+      }
+      ++ra;
+    }
+  }
+  // ---- force groups: the terms with a member in each 32-atom group ----
+  {
+    const int ng = (n + kForceGroup - 1) / kForceGroup;
+    std::vector<std::vector<int>> refs(ng);
+    auto add = [&](int kind, int t, const int* members, int nm) {
+      int last = -1;
+      for (int m = 0; m < nm; ++m) {
+        const int g = members[m] / kForceGroup;
+        bool seen = false;
+        for (int q = 0; q < m; ++q) seen = seen || members[q] / kForceGroup == g;
+        if (!seen) refs[g].push_back((kind << 29) | t);
+        last = g;
+      }
+      (void)last;
+    };
+    for (int t = 0; t < (int)L->bonds.size(); ++t) {
+      const int mm[2] = {L->bonds[t].i, L->bonds[t].j};
+      add(kRefBond, t, mm, 2);
+    }
+    for (int t = 0; t < (int)L->angles.size(); ++t) {
+      const int mm[3] = {L->angles[t].i, L->angles[t].j, L->angles[t].k};
+      add(kRefAngle, t, mm, 3);
+    }
+    for (int t = 0; t < (int)L->dihs.size(); ++t) {
+      const int mm[4] = {L->dihs[t].i, L->dihs[t].j, L->dihs[t].k, L->dihs[t].l};
+      add(kRefDih, t, mm, 4);
+    }
+    if ((int64_t)L->excs.size() >= (1 << 29)) return fail(PRISMQ_E_INVALID, "too many exceptions");
+    for (int t = 0; t < (int)L->excs.size(); ++t) {
+      const int mm[2] = {L->excs[t].i, L->excs[t].j};
+      add(kRefExc, t, mm, 2);
+    }
+    L->grp.resize(ng);
+    for (int g = 0; g < ng; ++g) {
+      L->grp[g] = make_int2((int)L->grp_refs.size(), (int)refs[g].size());
+      L->grp_refs.insert(L->grp_refs.end(), refs[g].begin(), refs[g].end());
+      int slots = 0;
+      for (int a = g * kForceGroup; a < std::min(n, (g + 1) * kForceGroup); ++a)
+        slots += (int)(ib[a].size() + ia[a].size() + id[a].size() + exc[a].size());
+      L->max_group_slots = std::max(L->max_group_slots, slots);
+    }
+    if (L->max_group_slots > kMaxGroupSlots)
+      return fail(PRISMQ_E_INVALID, "more than " + std::to_string(kMaxGroupSlots) +
+                                        " bonded and exception incidences in one 32-atom group");
   }
   // ---- exclusion window masks ----
   L->mask_all.assign(n, 0ull);
@@ -495,6 +562,8 @@ struct SlotRec {
   int64_t atom_b = 0, n_atoms = 0, unit_b = 0, n_units = 0;
   int64_t bond_b = 0, n_bonds = 0, angle_b = 0, n_angles = 0, dih_b = 0, n_dihs = 0;
   int64_t inc_b = 0, n_inc = 0, ex_b = 0, n_ex = 0, far_b = 0, n_far = 0, cell_b = 0, n_cell = 0;
+  int64_t exc_b = 0, n_exc = 0, gref_b = 0, n_gref = 0;
+  int max_group_slots = 0;
   bool ref_ok = false;
   bool need_prime = true;
   prismq_params params{};
@@ -504,7 +573,7 @@ struct SlotRec {
 
 struct prismq_batch {
   Arena A;
-  RangeAlloc r_atoms, r_units, r_bonds, r_angles, r_dihs, r_inc, r_ex, r_far, r_cells;
+  RangeAlloc r_atoms, r_units, r_bonds, r_angles, r_dihs, r_inc, r_ex, r_far, r_cells, r_exc, r_gref;
   std::vector<SlotRec> slots;
   cudaStream_t st = nullptr;
   cudaGraphExec_t gexec = nullptr;
@@ -519,12 +588,13 @@ struct prismq_batch {
   double* d_stage64 = nullptr;  // allocated on first FP64 read-back
   int precision = PRISMQ_PRECISION_FP32;
   int n_check32 = 0, n_check64 = 0;  // resident FP32 systems by constraint-check precision
+  int group_slots = 0;                // the largest force-group slot count among resident systems
   std::vector<SysDev> h_sys;
 
   ~prismq_batch() {
     if (gexec) cudaGraphExecDestroy(gexec);
     void* ptrs[] = {A.pos, A.vel, A.lj, A.xref, A.f, A.pe, A.atom_sys, A.mask_all, A.mask_ref, A.far,
-                    A.far_list, A.inc, A.inc_list, A.ex_idx, A.ex_partner, A.ex_par, A.bonds, A.angles,
+                    A.far_list, A.inc, A.inc_list, A.ex_idx, A.ex_partner, A.ex_par, A.exc, A.grp, A.grp_refs, A.bonds, A.angles,
                     A.dihs, A.units, A.noise, A.nbr, A.nnbr, A.cell_start, A.cell_atoms, A.atom_cell, A.work, A.work_ctl, A.sys,
                     A.pos64, A.vel64, A.f64, A.lj64, d_energy, d_stage, d_stage2, d_stage64};
     for (void* p : ptrs)
@@ -536,11 +606,15 @@ struct prismq_batch {
     const int64_t na = r_atoms.high(), nu = r_units.high();
     int ns = 0;
     int c32 = 0, c64 = 0;
+    int gs = 0;
     for (int i = 0; i < (int)slots.size(); ++i)
       if (slots[i].active) {
         ns = i + 1;
         (slots[i].params.constraint_check_fp64 ? c64 : c32) += 1;
+        gs = std::max(gs, slots[i].max_group_slots);
       }
+    if (gs != group_slots) graph_dirty = true;
+    group_slots = gs;
     if (na != atom_span || nu != unit_span || ns != sys_span) graph_dirty = true;
     if ((c32 > 0) != (n_check32 > 0) || (c64 > 0) != (n_check64 > 0)) graph_dirty = true;
     n_check32 = c32;
@@ -584,7 +658,7 @@ struct prismq_batch {
   void enqueue_step_body() {
     launch_control_cells(A, sys_span, kCtlStep, -1, st);
     launch_nbr_build(A, atom_span, 1, st);
-    launch_force(A, atom_span, false, st, false, force_variant);
+    launch_force(A, atom_span, false, st, false, force_variant, group_slots);
   }
 
   // Autotuner: time every force-kernel launch shape on the resident batch
@@ -600,9 +674,9 @@ struct prismq_batch {
     float best = 3.4e38f;
     int pick = 0;
     for (int v = 0; v < force_variant_count(); ++v) {
-      launch_force(A, atom_span, false, st, false, v);
+      launch_force(A, atom_span, false, st, false, v, group_slots);
       PQ_CK(cudaEventRecord(e0, st));
-      for (int r = 0; r < 3; ++r) launch_force(A, atom_span, false, st, false, v);
+      for (int r = 0; r < 3; ++r) launch_force(A, atom_span, false, st, false, v, group_slots);
       PQ_CK(cudaEventRecord(e1, st));
       PQ_CK(cudaEventSynchronize(e1));
       float ms = 0.f;
@@ -653,7 +727,7 @@ struct prismq_batch {
   prismq_status prime_flagged() {
     launch_control_cells(A, sys_span, kCtlPrime, -1, st);
     launch_nbr_build(A, atom_span, 1, st);
-    launch_force(A, atom_span, false, st, true);
+    launch_force(A, atom_span, false, st, true, 0, group_slots);
     g_launches += 3;
     PQ_CK(cudaGetLastError());
     for (auto& s : slots) s.need_prime = false;
@@ -703,7 +777,7 @@ struct prismq_batch {
       cudaEventRecordWithFlags(ev[4 * i + 1], st, cudaEventRecordExternal);
       launch_nbr_build(A, atom_span, 1, st);
       cudaEventRecordWithFlags(ev[4 * i + 2], st, cudaEventRecordExternal);
-      launch_force(A, atom_span, false, st, false, force_variant);
+      launch_force(A, atom_span, false, st, false, force_variant, group_slots);
       cudaEventRecordWithFlags(ev[4 * i + 3], st, cudaEventRecordExternal);
       integrate(kIntBoth);
     }
@@ -761,7 +835,8 @@ namespace {
 // receives the device bytes the same call would allocate.
 prismq_status batch_alloc(prismq_batch* B, int64_t atom_cap, int sys_cap, int64_t bond_cap,
                           int64_t angle_cap, int64_t dih_cap, int64_t inc_cap, int64_t ex_cap,
-                          int64_t far_cap, int64_t cell_cap, int precision = PRISMQ_PRECISION_FP32,
+                          int64_t far_cap, int64_t cell_cap, int64_t exc_cap, int64_t gref_cap,
+                          int precision = PRISMQ_PRECISION_FP32,
                           bool dry = false, int64_t* bytes_out = nullptr) {
   int ndev = 0;
   if (!dry && (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)) {
@@ -780,6 +855,8 @@ prismq_status batch_alloc(prismq_batch* B, int64_t atom_cap, int sys_cap, int64_
   A.ex_cap = std::max<int64_t>(ex_cap, 1);
   A.far_cap = std::max<int64_t>(far_cap, 1);
   A.cell_cap = std::max<int64_t>(cell_cap, 1);
+  A.exc_cap = std::max<int64_t>(exc_cap, 1);
+  A.gref_cap = std::max<int64_t>(gref_cap, 1);
   A.sys_cap = sys_cap;
   if (!dry) PQ_CK(cudaStreamCreateWithFlags(&B->st, cudaStreamNonBlocking));
 #define PQ_ALLOC(ptr, count)                                  \
@@ -804,6 +881,9 @@ prismq_status batch_alloc(prismq_batch* B, int64_t atom_cap, int sys_cap, int64_
   PQ_ALLOC(A.ex_idx, atom_cap);
   PQ_ALLOC(A.ex_partner, A.ex_cap);
   PQ_ALLOC(A.ex_par, A.ex_cap);
+  PQ_ALLOC(A.exc, A.exc_cap);
+  PQ_ALLOC(A.grp, atom_cap / kForceGroup + 1);
+  PQ_ALLOC(A.grp_refs, A.gref_cap);
   PQ_ALLOC(A.bonds, A.bond_cap);
   PQ_ALLOC(A.angles, A.angle_cap);
   PQ_ALLOC(A.dihs, A.dih_cap);
@@ -834,6 +914,7 @@ prismq_status batch_alloc(prismq_batch* B, int64_t atom_cap, int sys_cap, int64_
   if (A.fp64) PQ_CK(cudaMemsetAsync(A.f64, 0, sizeof(double) * 3 * atom_cap, B->st));
   PQ_CK(cudaMemsetAsync(A.sys, 0, sizeof(SysDev) * sys_cap, B->st));
   PQ_CK(cudaMemsetAsync(A.nnbr, 0, sizeof(int) * atom_cap, B->st));
+  PQ_CK(cudaMemsetAsync(A.grp, 0, sizeof(int2) * (atom_cap / kForceGroup + 1), B->st));
   PQ_CK(cudaMemsetAsync(A.work_ctl, 0, sizeof(int) * 4, B->st));
   PQ_CK(cudaMemsetAsync(A.f, 0, sizeof(long long) * 3 * atom_cap, B->st));
   PQ_CK(cudaMemsetAsync(A.pe, 0, sizeof(double) * 5 * atom_cap, B->st));
@@ -850,6 +931,8 @@ prismq_status batch_alloc(prismq_batch* B, int64_t atom_cap, int sys_cap, int64_
   B->r_ex.init(A.ex_cap);
   B->r_far.init(A.far_cap);
   B->r_cells.init(A.cell_cap);
+  B->r_exc.init(A.exc_cap);
+  B->r_gref.init(A.gref_cap);
   B->slots.resize(sys_cap);
   B->h_sys.resize(sys_cap);
   return PRISMQ_OK;
@@ -863,7 +946,7 @@ prismq_status batch_alloc_sized(prismq_batch* B, int64_t max_atoms, int32_t max_
                                 int64_t* bytes_out, int precision = PRISMQ_PRECISION_FP32) {
   const int64_t na = (max_atoms + 31) / 32 * 32 + 32 * (int64_t)max_systems;
   return batch_alloc(B, na, max_systems, 2 * na, 4 * na, 8 * na, 48 * na, 8 * na, 2 * na,
-                     2 * (na / 2 + 1026 * (int64_t)max_systems), precision, dry, bytes_out);
+                     2 * (na / 2 + 1026 * (int64_t)max_systems), 4 * na, 16 * na, precision, dry, bytes_out);
 }
 
 template <class T>
@@ -894,6 +977,9 @@ prismq_status batch_admit(prismq_batch* B, const Lowered& L0, const prismq_param
   R.n_ex = (int64_t)L.ex_partner.size();
   R.n_far = (int64_t)L.far_list.size();
   R.n_cell = 2 * ((int64_t)L.cell_cap + 1);
+  R.n_exc = (int64_t)L.excs.size();
+  R.n_gref = (int64_t)L.grp_refs.size();
+  R.max_group_slots = L.max_group_slots;
   struct Req {
     RangeAlloc* r;
     int64_t n;
@@ -903,7 +989,8 @@ prismq_status batch_admit(prismq_batch* B, const Lowered& L0, const prismq_param
               {&B->r_bonds, R.n_bonds, &R.bond_b, 1},  {&B->r_angles, R.n_angles, &R.angle_b, 1},
               {&B->r_dihs, R.n_dihs, &R.dih_b, 1},     {&B->r_inc, R.n_inc, &R.inc_b, 1},
               {&B->r_ex, R.n_ex, &R.ex_b, 1},          {&B->r_far, R.n_far, &R.far_b, 1},
-              {&B->r_cells, R.n_cell, &R.cell_b, 1}};
+              {&B->r_cells, R.n_cell, &R.cell_b, 1},   {&B->r_exc, R.n_exc, &R.exc_b, 1},
+              {&B->r_gref, R.n_gref, &R.gref_b, 1}};
   int done = 0;
   for (auto& q : reqs) {
     const int64_t b = q.r->alloc(q.n, q.align);
@@ -944,6 +1031,16 @@ prismq_status batch_admit(prismq_batch* B, const Lowered& L0, const prismq_param
     L.far[a].x += (int)R.far_b;
   }
   for (auto& j : L.ex_partner) j += ab;
+  for (auto& e : L.excs) {
+    e.i += ab;
+    e.j += ab;
+  }
+  for (auto& r : L.grp_refs) {
+    const int kind = r >> 29, t = r & ((1 << 29) - 1);
+    const int64_t base = kind == kRefBond ? R.bond_b : kind == kRefAngle ? R.angle_b : kind == kRefDih ? R.dih_b : R.exc_b;
+    r = (kind << 29) | (int)(t + base);
+  }
+  for (auto& g : L.grp) g.x += (int)R.gref_b;
   for (auto& e : L.far_list) e = ((e & 0x3fffffff) + ab) | (e & 0x40000000);
   for (auto& U : L.units) {
     for (int k = 0; k < 4; ++k)
@@ -974,6 +1071,9 @@ prismq_status batch_admit(prismq_batch* B, const Lowered& L0, const prismq_param
   PQ_UP(A.angles + R.angle_b, L.angles);
   PQ_UP(A.dihs + R.dih_b, L.dihs);
   PQ_UP(A.units + R.unit_b, L.units);
+  PQ_UP(A.exc + R.exc_b, L.excs);
+  PQ_UP(A.grp_refs + R.gref_b, L.grp_refs);
+  PQ_UP(A.grp + ab / kForceGroup, L.grp);
 #undef PQ_UP
   if (A.fp64) {
     std::vector<double4_32a> p64(L.n), v64(L.n);
@@ -1029,6 +1129,8 @@ prismq_status batch_release(prismq_batch* B, int slot) {
   PQ_CK(cudaMemsetAsync(A.atom_sys + R.atom_b, 0xff, sizeof(int) * R.n_atoms, st));
   if (R.n_units)
     k_deactivate_units<<<(unsigned)((R.n_units + 255) / 256), 256, 0, st>>>(A.units + R.unit_b, R.n_units);
+  PQ_CK(cudaMemsetAsync(A.grp + R.atom_b / kForceGroup, 0,
+                        sizeof(int2) * ((R.n_atoms + kForceGroup - 1) / kForceGroup), st));
   PQ_CK(cudaMemsetAsync(A.sys + slot, 0, sizeof(SysDev), st));
   PQ_CK(cudaStreamSynchronize(st));
   B->r_atoms.release(R.atom_b, R.n_atoms);
@@ -1040,6 +1142,8 @@ prismq_status batch_release(prismq_batch* B, int slot) {
   B->r_ex.release(R.ex_b, R.n_ex);
   B->r_far.release(R.far_b, R.n_far);
   B->r_cells.release(R.cell_b, R.n_cell);
+  B->r_exc.release(R.exc_b, R.n_exc);
+  B->r_gref.release(R.gref_b, R.n_gref);
   R = SlotRec();
   B->update_spans();
   return PRISMQ_OK;
@@ -1091,10 +1195,10 @@ prismq_status check_slot(prismq_batch* B, int slot) {
 prismq_status eval_energy(prismq_batch* B, int slot, double* out15) {
   prismq_status rc = B->prime_if_needed();
   if (rc != PRISMQ_OK) return rc;
-  launch_force(B->A, B->atom_span, true, B->st);
+  launch_force(B->A, B->atom_span, true, B->st, false, 0, B->group_slots);
   launch_energy_reduce(B->A, B->sys_span, B->d_energy, B->st);
   // the stepping kernels consume forces from the force-only variant
-  launch_force(B->A, B->atom_span, false, B->st);
+  launch_force(B->A, B->atom_span, false, B->st, false, 0, B->group_slots);
   g_launches += 3;
   PQ_CK(cudaGetLastError());
   if (out15) {
@@ -1411,7 +1515,8 @@ prismq_status prismq_system_create(const prismq_topology* topo, const prismq_par
   const int64_t n = L.n;
   rc = batch_alloc(B, n, 1, (int64_t)L.bonds.size(), (int64_t)L.angles.size(), (int64_t)L.dihs.size(),
                    (int64_t)L.inc_list.size(), (int64_t)L.ex_partner.size(), (int64_t)L.far_list.size(),
-                   2 * ((int64_t)L.cell_cap + 1), params->precision);
+                   2 * ((int64_t)L.cell_cap + 1), (int64_t)L.excs.size(), (int64_t)L.grp_refs.size(),
+                   params->precision);
   if (rc != PRISMQ_OK) {
     delete B;
     return rc;
@@ -1563,7 +1668,7 @@ prismq_status prismq_build_neighbors(prismq_system* sys, prismq_nlist_mode mode,
     return fail(PRISMQ_E_INVALID, "reference grid needs more than 32 cells per axis for this system");
   launch_control_cells(B->A, B->sys_span, kCtlForce, (int)mode, B->st);
   launch_nbr_build(B->A, B->atom_span, 0, B->st);
-  launch_force(B->A, B->atom_span, false, B->st);  // also clears the rebuild queue
+  launch_force(B->A, B->atom_span, false, B->st, false, 0, B->group_slots);  // also clears the rebuild queue
   g_launches += 3;
   PQ_CK(cudaGetLastError());
   const int64_t n = R.n_atoms, ab = R.atom_b;
@@ -1578,7 +1683,7 @@ prismq_status prismq_build_neighbors(prismq_system* sys, prismq_nlist_mode mode,
   // restore the production list
   launch_control_cells(B->A, B->sys_span, kCtlForce, 0, B->st);
   launch_nbr_build(B->A, B->atom_span, 1, B->st);
-  launch_force(B->A, B->atom_span, false, B->st);
+  launch_force(B->A, B->atom_span, false, B->st, false, 0, B->group_slots);
   g_launches += 3;
   PQ_CK(cudaGetLastError());
   PQ_CK(cudaStreamSynchronize(B->st));

@@ -25,6 +25,8 @@
 // the same decomposition with double positions, double pair and bonded math
 // and double accumulation (lanes summed by the same fixed butterfly), writing
 // the FP64 force planes.
+#include <algorithm>
+
 #include "pq_common.cuh"
 #include "pq_device.cuh"
 
@@ -264,71 +266,267 @@ __device__ __forceinline__ void store_force(const Arena& A, int a, const Acc<dou
   }
 }
 
-// Four lanes per atom: lane q takes bonded terms, exceptions and row entries
-// with index ≡ q (mod 4).  Each lane keeps FP32 partial sums over at most 32 of
-// its entries and accumulates them in int64; the lanes' int64 totals are then
-// summed exactly.  The decomposition depends only on the atom's own lists, so
-// an atom's force is identical whatever batch it is computed in.
-template <class R, bool kEnergy, int kBlock, int kMinBlocks>
-__global__ void __launch_bounds__(kBlock, kMinBlocks) k_force(Arena A, int64_t n_span, int only_rebuilt) {
+// ---- per-term contributions, as each member's gather adds them ----
+//
+// A term is evaluated once; member m's contribution is the value the member
+// would add to its own force (the per-member laws above: bond s*r with
+// s = -fm or fm, angle -(fm*d) for the ends and fm*(di+dk) for the apex,
+// torsion f1, s-f1, -s-f4, f4; exceptions -(fs*d) seen from either member,
+// d = x_partner - x_self, which is the same number negated).
+template <class R>
+struct TermOut {
+  R x[4], y[4], z[4];
+  double e;  // energy share of every member
+};
+
+template <class R>
+__device__ __forceinline__ bool bond_out(const R4<R>* pos, const BondT b, TermOut<R>& o) {
+  const R4<R> pi = pos[b.i], pj = pos[b.j];
+  const R rx = pj.x - pi.x, ry = pj.y - pi.y, rz = pj.z - pi.z;
+  const R r = sqrt_r(rx * rx + ry * ry + rz * rz);
+  if (r < R(1e-8f)) return false;
+  const R dr = r - R(b.r0);
+  const R fm = R(-2.0f) * R(b.k) * dr / r;
+  const R sn = -fm;
+  o.x[0] = sn * rx; o.y[0] = sn * ry; o.z[0] = sn * rz;
+  o.x[1] = fm * rx; o.y[1] = fm * ry; o.z[1] = fm * rz;
+  o.e = (double)b.k * (double)dr * (double)dr * 0.5;
+  return true;
+}
+
+template <class R>
+__device__ __forceinline__ bool angle_out(const R4<R>* pos, const AngleT a, TermOut<R>& o) {
+  const R4<R> pi = pos[a.i], pj = pos[a.j], pk = pos[a.k];
+  const R ax = pi.x - pj.x, ay = pi.y - pj.y, az = pi.z - pj.z;  // rij
+  const R bx = pk.x - pj.x, by = pk.y - pj.y, bz = pk.z - pj.z;  // rkj
+  const R la = sqrt_r(ax * ax + ay * ay + az * az);
+  const R lb = sqrt_r(bx * bx + by * by + bz * bz);
+  if (la < R(1e-8f) || lb < R(1e-8f)) return false;
+  R c = (ax * bx + ay * by + az * bz) / (la * lb);
+  c = max_r(R(-1.0f), min_r(R(1.0f), c));
+  const R th = acos_r(c);
+  const R dth = th - R(a.theta0);
+  R sn = sqrt_r(R(1.0f) - c * c);
+  if (sn < R(1e-8f)) sn = R(1e-8f);
+  const R fm = R(-2.0f) * R(a.kf) * dth / sn;
+  const R ia = R(1.0f) / la, ib = R(1.0f) / lb;
+  const R dix = (bx * ib - c * ax * ia) * ia, diy = (by * ib - c * ay * ia) * ia, diz = (bz * ib - c * az * ia) * ia;
+  const R dkx = (ax * ia - c * bx * ib) * ib, dky = (ay * ia - c * by * ib) * ib, dkz = (az * ia - c * bz * ib) * ib;
+  o.x[0] = -(fm * dix); o.y[0] = -(fm * diy); o.z[0] = -(fm * diz);
+  o.x[2] = -(fm * dkx); o.y[2] = -(fm * dky); o.z[2] = -(fm * dkz);
+  o.x[1] = fm * (dix + dkx); o.y[1] = fm * (diy + dky); o.z[1] = fm * (diz + dkz);
+  o.e = (double)a.kf * (double)dth * (double)dth * (1.0 / 3.0);
+  return true;
+}
+
+template <class R>
+__device__ __forceinline__ bool dihedral_out(const R4<R>* pos, const DihT d, TermOut<R>& o) {
+  const R4<R> pi = pos[d.i], pj = pos[d.j], pk = pos[d.k], pl = pos[d.l];
+  const R v0x = pi.x - pj.x, v0y = pi.y - pj.y, v0z = pi.z - pj.z;
+  const R v1x = pk.x - pj.x, v1y = pk.y - pj.y, v1z = pk.z - pj.z;
+  const R v2x = pk.x - pl.x, v2y = pk.y - pl.y, v2z = pk.z - pl.z;
+  const R c0x = v0y * v1z - v0z * v1y, c0y = v0z * v1x - v0x * v1z, c0z = v0x * v1y - v0y * v1x;
+  const R c1x = v1y * v2z - v1z * v2y, c1y = v1z * v2x - v1x * v2z, c1z = v1x * v2y - v1y * v2x;
+  const R n1 = c0x * c0x + c0y * c0y + c0z * c0z;
+  const R n2 = c1x * c1x + c1y * c1y + c1z * c1z;
+  const R nb = v1x * v1x + v1y * v1y + v1z * v1z;
+  if (n1 < R(1e-16f) || n2 < R(1e-16f) || nb < R(1e-16f)) return false;
+  const R lbc = sqrt_r(nb);
+  R cp = (c0x * c1x + c0y * c1y + c0z * c1z) / sqrt_r(n1 * n2);
+  cp = max_r(R(-1.0f), min_r(R(1.0f), cp));
+  R phi;
+  if (cp > R(0.99f) || cp < R(-0.99f)) {
+    const R xx = c0y * c1z - c0z * c1y, xy = c0z * c1x - c0x * c1z, xz = c0x * c1y - c0y * c1x;
+    R s2 = (xx * xx + xy * xy + xz * xz) / (n1 * n2);
+    s2 = max_r(R(0.0f), min_r(R(1.0f), s2));
+    phi = asin_r(sqrt_r(s2));
+    if (cp < R(0.0f)) phi = R(3.14159265358979323846) - phi;
+  } else {
+    phi = acos_r(cp);
+  }
+  if (v0x * c1x + v0y * c1y + v0z * c1z < R(0.0f)) phi = -phi;
+  const R n = (R)d.n;
+  const R dE = -R(d.kf) * n * sin_r(n * phi - R(d.phase));
+  const R inb = R(1.0f) / nb;
+  const R ff0 = (-dE * lbc) / n1;
+  const R ff1 = (v0x * v1x + v0y * v1y + v0z * v1z) * inb;
+  const R ff2 = (v2x * v1x + v2y * v1y + v2z * v1z) * inb;
+  const R ff3 = (dE * lbc) / n2;
+  const R f1x = ff0 * c0x, f1y = ff0 * c0y, f1z = ff0 * c0z;
+  const R f4x = ff3 * c1x, f4y = ff3 * c1y, f4z = ff3 * c1z;
+  const R sx = ff1 * f1x - ff2 * f4x, sy = ff1 * f1y - ff2 * f4y, sz = ff1 * f1z - ff2 * f4z;
+  o.x[0] = f1x; o.y[0] = f1y; o.z[0] = f1z;
+  o.x[1] = sx - f1x; o.y[1] = sy - f1y; o.z[1] = sz - f1z;
+  o.x[2] = -sx - f4x; o.y[2] = -sy - f4y; o.z[2] = -sz - f4z;
+  o.x[3] = f4x; o.y[3] = f4y; o.z[3] = f4z;
+  o.e = (double)d.kf * (1.0 + cos((double)n * (double)phi - (double)d.phase)) * 0.25;
+  return true;
+}
+
+// exact exceptions: no cutoff, no shift (nhs_amber_fused.cu:3316-3467)
+template <class R>
+__device__ __forceinline__ bool exception_out(const R4<R>* pos, const ExcT e, TermOut<R>& o, bool& bad) {
+  const R4<R> pi = pos[e.i], pj = pos[e.j];
+  const R dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+  const R r2 = fma_r(dz, dz, fma_r(dy, dy, dx * dx));
+  if (r2 < R(1e-8f)) {
+    bad = true;
+    return false;
+  }
+  R inv_r, s6;
+  const R fs = pair_scalar<R>(r2, R(e.sig), R(e.eps), R(e.qq), inv_r, s6);
+  const R px = fs * dx, py = fs * dy, pz = fs * dz;
+  o.x[0] = -px; o.y[0] = -py; o.z[0] = -pz;
+  o.x[1] = px; o.y[1] = py; o.z[1] = pz;
+  o.e = (4.0 * (double)e.eps * ((double)s6 * (double)s6 - (double)s6) +
+         (double)kCoulomb * (double)e.qq * (double)inv_r) * 0.5;
+  return true;
+}
+
+// One force block = one 32-atom group, four lanes per atom.
+//   1. The block evaluates every bonded term and exception pair with a member
+//      in the group once (one thread per term), and drops each member's
+//      contribution into a shared-memory slot: the member's incidence entries
+//      of each kind, in the order the member lists them.
+//   2. Lane q of an atom sums the slots of its entries with index ≡ q (mod 4),
+//      bonded kinds first, then exceptions, then its row entries ≡ q (mod 4).
+// Each lane keeps FP32 partial sums over at most 32 of its entries and
+// accumulates them in int64; the lanes' int64 totals are then summed exactly.
+// The decomposition depends only on the atom's own lists, so an atom's force
+// is identical whatever batch it is computed in.  The reference recomputes
+// each term for every member atom (nhs_amber_fused.cu:3002-3090); evaluating
+// it once per group gives each member the same contribution.
+template <class R, bool kEnergy, int kMinBlocks>
+__global__ void __launch_bounds__(128, kMinBlocks) k_force(Arena A, int64_t n_span, int only_rebuilt, int cap) {
   // the row builder that ran before this launch consumed the rebuild queue
   if (blockIdx.x == 0 && threadIdx.x == 0) A.work_ctl[0] = 0;
-  const int64_t a64 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 2;
-  const int q = threadIdx.x & 3;
-  bool live = a64 < n_span;
-  const int a = live ? (int)a64 : 0;
-  const int s = live ? A.atom_sys[a] : -1;
-  live = live && s >= 0;
-  const SysDev* Sp = live ? &A.sys[s] : nullptr;
-  live = live && Sp->active && (!only_rebuilt || Sp->rebuilding);
-  // all four lanes of an atom share `live`; whole quads leave together
-  if (!live) return;
-  const R cut2 = R(Sp->cut2);
+  extern __shared__ __align__(16) unsigned char force_smem[];
+  __shared__ int s_base[kForceGroup], s_nb[kForceGroup], s_na[kForceGroup], s_nd[kForceGroup];
+  const int tid = threadIdx.x, q = tid & 3;
+  const int64_t a0 = (int64_t)blockIdx.x * kForceGroup;
+  if (a0 >= n_span) return;
+  const int s0 = A.atom_sys[a0];
+  if (s0 < 0) return;
+  const SysDev* Sp = &A.sys[s0];
+  if (!Sp->active || (only_rebuilt && !Sp->rebuilding)) return;  // whole block leaves together
+  R* slot_x = reinterpret_cast<R*>(force_smem);
+  R* slot_y = slot_x + cap;
+  R* slot_z = slot_y + cap;
+  double* slot_e = reinterpret_cast<double*>(slot_z + cap);
+  // ---- slot layout of the group's atoms ----
+  if (tid < kForceGroup) {
+    const int64_t b = a0 + tid;
+    int nb = 0, na = 0, nd = 0, ne = 0;
+    if (b < n_span && A.atom_sys[b] == s0) {
+      const Incidence I = A.inc[b];
+      nb = I.counts & 0xff;
+      na = (I.counts >> 8) & 0xff;
+      nd = (I.counts >> 16) & 0xff;
+      ne = A.ex_idx[b].y;
+    }
+    const int tot = nb + na + nd + ne;
+    int incl = tot;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (tid >= o) incl += v;
+    }
+    s_base[tid] = incl - tot;
+    s_nb[tid] = nb;
+    s_na[tid] = na;
+    s_nd[tid] = nd;
+  }
+  __syncthreads();
   const R4<R>* pos = positions(A, R(0));
+  // ---- every term with a member in the group, once ----
+  const int2 gr = A.grp[blockIdx.x];
+  bool bad = false;
+  for (int r = tid; r < gr.y; r += 128) {
+    const int ref = A.grp_refs[gr.x + r];
+    const int kind = ref >> 29, t = ref & ((1 << 29) - 1);
+    TermOut<R> o;
+    int mem[4], pp[4], nm, koff;  // koff: 0 bonds, 1 angles, 2 torsions, 3 exceptions
+    bool ok;
+    if (kind == kRefBond) {
+      const BondT b = A.bonds[t];
+      ok = bond_out<R>(pos, b, o);
+      nm = 2; mem[0] = b.i; mem[1] = b.j; pp[0] = b.pos & 0xffff; pp[1] = b.pos >> 16;
+    } else if (kind == kRefAngle) {
+      const AngleT g = A.angles[t];
+      ok = angle_out<R>(pos, g, o);
+      nm = 3; mem[0] = g.i; mem[1] = g.j; mem[2] = g.k;
+      pp[0] = g.pos & 1023; pp[1] = (g.pos >> 10) & 1023; pp[2] = (g.pos >> 20) & 1023;
+    } else if (kind == kRefDih) {
+      const DihT d = A.dihs[t];
+      ok = dihedral_out<R>(pos, d, o);
+      nm = 4; mem[0] = d.i; mem[1] = d.j; mem[2] = d.k; mem[3] = d.l;
+      pp[0] = d.pos & 255; pp[1] = (d.pos >> 8) & 255; pp[2] = (d.pos >> 16) & 255; pp[3] = (d.pos >> 24) & 255;
+    } else {
+      const ExcT e = A.exc[t];
+      ok = exception_out<R>(pos, e, o, bad);
+      nm = 2; mem[0] = e.i; mem[1] = e.j; pp[0] = e.pos & 0xffff; pp[1] = e.pos >> 16;
+    }
+    koff = kind;
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      if (m >= nm) break;
+      const int li = (int)(mem[m] - a0);
+      if (li < 0 || li >= kForceGroup) continue;
+      const int off = koff == 0 ? 0 : koff == 1 ? s_nb[li] : koff == 2 ? s_nb[li] + s_na[li]
+                                                               : s_nb[li] + s_na[li] + s_nd[li];
+      const int sl = s_base[li] + off + pp[m];
+      if (sl >= cap) {  // cannot happen: cap covers the fullest group
+        bad = true;
+        continue;
+      }
+      slot_x[sl] = ok ? o.x[m] : R(0.0f);
+      slot_y[sl] = ok ? o.y[m] : R(0.0f);
+      slot_z[sl] = ok ? o.z[m] : R(0.0f);
+      if (kEnergy) slot_e[sl] = ok ? o.e : 0.0;
+    }
+  }
+  if (bad) atomicOr(&A.sys[s0].status, kStNonfinite);
+  __syncthreads();
+  const int ga = tid >> 2;  // the thread's atom within the group
+  const int64_t a64 = a0 + ga;
+  if (a64 >= n_span || A.atom_sys[a64] != s0) return;
+  const int a = (int)a64;
+  const R cut2 = R(Sp->cut2);
   Acc<R> f{};
   double eb = 0.0, ea = 0.0, ed = 0.0, ex = 0.0, en = 0.0;
-
-  const Incidence I = A.inc[a];
-  const int nb = I.counts & 0xff, na = (I.counts >> 8) & 0xff, nd = (I.counts >> 16) & 0xff;
-  for (int t = q; t < nb; t += kLanes) {
-    const int ent = A.inc_list[I.b_beg + t];
-    bond_term<R>(pos, A.bonds[ent >> 2], ent & 3, f, kEnergy ? &eb : nullptr);
+  {
+    const int base = s_base[ga], nb = s_nb[ga], na = s_na[ga], nd = s_nd[ga];
+    for (int t = q; t < nb; t += kLanes) {
+      f.x += slot_x[base + t];
+      f.y += slot_y[base + t];
+      f.z += slot_z[base + t];
+      if (kEnergy) eb += slot_e[base + t];
+    }
+    for (int t = q; t < na; t += kLanes) {
+      const int sl = base + nb + t;
+      f.x += slot_x[sl];
+      f.y += slot_y[sl];
+      f.z += slot_z[sl];
+      if (kEnergy) ea += slot_e[sl];
+    }
+    for (int t = q; t < nd; t += kLanes) {
+      const int sl = base + nb + na + t;
+      f.x += slot_x[sl];
+      f.y += slot_y[sl];
+      f.z += slot_z[sl];
+      if (kEnergy) ed += slot_e[sl];
+    }
+    f.flush();
+    const int ne = A.ex_idx[a].y;
+    for (int t = q; t < ne; t += kLanes) {
+      const int sl = base + nb + na + nd + t;
+      f.x += slot_x[sl];
+      f.y += slot_y[sl];
+      f.z += slot_z[sl];
+      if (kEnergy) ex += slot_e[sl];
+    }
+    f.flush();
   }
-  for (int t = q; t < na; t += kLanes) {
-    const int ent = A.inc_list[I.a_beg + t];
-    angle_term<R>(pos, A.angles[ent >> 2], ent & 3, f, kEnergy ? &ea : nullptr);
-  }
-  for (int t = q; t < nd; t += kLanes) {
-    const int ent = A.inc_list[I.d_beg + t];
-    dihedral_term<R>(pos, A.dihs[ent >> 2], ent & 3, f, kEnergy ? &ed : nullptr);
-  }
-  f.flush();
-
   const R4<R> pi = pos[a];
-  // exact exceptions: no cutoff, no shift (nhs_amber_fused.cu:3316-3467)
-  const int2 xr = A.ex_idx[a];
-  for (int t = q; t < xr.y; t += kLanes) {
-    const int j = A.ex_partner[xr.x + t];
-    const float4 par = A.ex_par[xr.x + t];
-    const R4<R> pj = pos[j];
-    const R dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
-    const R r2 = fma_r(dz, dz, fma_r(dy, dy, dx * dx));
-    if (r2 < R(1e-8f)) {
-      atomicOr(&A.sys[s].status, kStNonfinite);
-      continue;
-    }
-    R inv_r, s6;
-    const R fs = pair_scalar<R>(r2, R(par.y), R(par.z), R(par.x), inv_r, s6);
-    f.x -= fs * dx;
-    f.y -= fs * dy;
-    f.z -= fs * dz;
-    if (kEnergy) {
-      const double v = 4.0 * (double)par.z * ((double)s6 * (double)s6 - (double)s6) +
-                       (double)kCoulomb * (double)par.x * (double)inv_r;
-      ex += v * 0.5;
-    }
-  }
-  f.flush();
 
   // ordinary pairs: lane q walks entries q, q+4, ... of the tiled row
   const R2<R>* ljp = lj_params(A, R(0));
@@ -415,13 +613,13 @@ __global__ void __launch_bounds__(kBlock, kMinBlocks) k_force(Arena A, int64_t n
   }
 }
 
-// Launch shapes of the force-only kernel the autotuner chooses from: threads per
-// block and the minimum resident blocks per SM handed to the register allocator.
+// Launch shapes of the force-only kernel the autotuner chooses from: the
+// minimum resident 128-thread blocks per SM handed to the register allocator.
 // The shape changes neither the per-atom decomposition nor the results.
 struct ForceShape {
   int block, min_blocks;
 };
-static const ForceShape kForceShapes[] = {{128, 1}, {128, 12}, {256, 6}, {64, 24}};
+static const ForceShape kForceShapes[] = {{128, 1}, {128, 8}, {128, 12}};
 
 int force_variant_count() { return (int)(sizeof(kForceShapes) / sizeof(kForceShapes[0])); }
 
@@ -430,29 +628,39 @@ void force_variant_shape(int v, int* block, int* min_blocks) {
   *min_blocks = kForceShapes[v].min_blocks;
 }
 
+template <class R, bool kEnergy, int kMinBlocks>
+static void force_launch(const Arena& A, int64_t n, int ob, int cap, cudaStream_t st) {
+  const size_t smem = (size_t)cap * (3 * sizeof(R) + (kEnergy ? sizeof(double) : 0));
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_force<R, kEnergy, kMinBlocks>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)((size_t)kMaxGroupSlots * (3 * sizeof(R) + sizeof(double))));
+    attr = true;
+  }
+  const unsigned blocks = (unsigned)((n + kForceGroup - 1) / kForceGroup);
+  k_force<R, kEnergy, kMinBlocks><<<blocks, 128, smem, st>>>(A, n, ob, cap);
+}
+
 void launch_force(const Arena& A, int64_t n_atoms_span, bool energy, cudaStream_t st, bool only_rebuilt,
-                  int variant) {
+                  int variant, int group_slots) {
   if (n_atoms_span <= 0) return;
   const int ob = only_rebuilt ? 1 : 0;
-  const unsigned blocks128 = (unsigned)((n_atoms_span * kLanes + 127) / 128);
+  const int cap = (std::max(group_slots, 1) + 7) & ~7;  // keeps the FP64 energy plane 8-byte aligned
   if (A.fp64) {
     if (energy)
-      k_force<double, true, 128, 1><<<blocks128, 128, 0, st>>>(A, n_atoms_span, ob);
+      force_launch<double, true, 1>(A, n_atoms_span, ob, cap, st);
     else
-      k_force<double, false, 128, 1><<<blocks128, 128, 0, st>>>(A, n_atoms_span, ob);
+      force_launch<double, false, 1>(A, n_atoms_span, ob, cap, st);
     return;
   }
   if (energy) {
-    k_force<float, true, 128, 1><<<blocks128, 128, 0, st>>>(A, n_atoms_span, ob);
+    force_launch<float, true, 1>(A, n_atoms_span, ob, cap, st);
     return;
   }
-  const int bs = kForceShapes[variant].block;
-  const unsigned blocks = (unsigned)((n_atoms_span * kLanes + bs - 1) / bs);
   switch (variant) {
-    case 1: k_force<float, false, 128, 12><<<blocks, 128, 0, st>>>(A, n_atoms_span, ob); break;
-    case 2: k_force<float, false, 256, 6><<<blocks, 256, 0, st>>>(A, n_atoms_span, ob); break;
-    case 3: k_force<float, false, 64, 24><<<blocks, 64, 0, st>>>(A, n_atoms_span, ob); break;
-    default: k_force<float, false, 128, 1><<<blocks, 128, 0, st>>>(A, n_atoms_span, ob); break;
+    case 1: force_launch<float, false, 8>(A, n_atoms_span, ob, cap, st); break;
+    case 2: force_launch<float, false, 12>(A, n_atoms_span, ob, cap, st); break;
+    default: force_launch<float, false, 1>(A, n_atoms_span, ob, cap, st); break;
   }
 }
 

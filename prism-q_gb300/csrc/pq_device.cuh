@@ -31,19 +31,37 @@ constexpr int kStCellOverflow = 4;
 constexpr int kStNbrOverflow = 8;
 constexpr int kStNonfinite = 16;
 
+// Bonded terms carry, per member, the term's position in that member's
+// incidence list of its kind (`pos`), so a term evaluated once can drop each
+// member's contribution into the slot that member's gather reads.
 struct BondT {
   int i, j;
   float r0, k;
+  int pos;  // pos_i | pos_j << 16
 };
 struct AngleT {
   int i, j, k;
   float theta0, kf;
+  int pos;  // pos_i | pos_j << 10 | pos_k << 20
 };
 struct DihT {
   int i, j, k, l;
   int n;
   float phase, kf;
+  int pos;  // 8 bits per member
 };
+// One exact 1-4 exception pair (each pair once), with its rank in each
+// member's ascending exception list.
+struct ExcT {
+  int i, j;
+  float qq, sig, eps;
+  int pos;  // pos_i | pos_j << 16
+};
+
+// Kinds of the per-group term references (ref = kind << 29 | term index).
+constexpr int kRefBond = 0, kRefAngle = 1, kRefDih = 2, kRefExc = 3;
+constexpr int kForceGroup = 32;  // atoms per force block (128 threads, 4 lanes per atom)
+constexpr int kMaxGroupSlots = 2048;  // bonded + exception incidences of one group (shared-memory slots)
 
 // A constraint unit: one H cluster (central + up to 3 H) or one lone atom.
 struct Unit {
@@ -102,7 +120,7 @@ struct Incidence {
 
 struct Arena {
   int64_t atom_cap = 0, unit_cap = 0, bond_cap = 0, angle_cap = 0, dih_cap = 0, inc_cap = 0,
-          ex_cap = 0, far_cap = 0, cell_cap = 0;
+          ex_cap = 0, far_cap = 0, cell_cap = 0, exc_cap = 0, gref_cap = 0;
   int sys_cap = 0;
   // per atom
   float4* pos = nullptr;   // x y z q
@@ -121,6 +139,11 @@ struct Arena {
   int2* ex_idx = nullptr;     // {begin, count}
   int* ex_partner = nullptr;  // global partner index
   float4* ex_par = nullptr;   // qq, sigma, epsilon, 0
+  ExcT* exc = nullptr;        // exception pairs, each once
+  // per 32-atom force group: {begin, count} into grp_refs, the terms with a
+  // member in the group
+  int2* grp = nullptr;
+  int* grp_refs = nullptr;
   // terms
   BondT* bonds = nullptr;
   AngleT* angles = nullptr;
@@ -166,8 +189,10 @@ void launch_control_cells(const Arena& A, int n_sys, int mode, int nbr_mode_over
                           cudaStream_t st);
 void launch_nbr_build(const Arena& A, int64_t n_atoms_span, int exclude_exceptions,
                       cudaStream_t st);
+// group_slots: the largest number of bonded + exception incidences of one
+// 32-atom group among the resident systems (sizes the shared-memory slots).
 void launch_force(const Arena& A, int64_t n_atoms_span, bool energy, cudaStream_t st,
-                  bool only_rebuilt = false, int variant = 0);
+                  bool only_rebuilt = false, int variant = 0, int group_slots = 0);
 int force_variant_count();
 void force_variant_shape(int variant, int* block, int* min_blocks);
 // check64_pass: 0 = systems with FP32 constraint checks, 1 = systems with FP64
