@@ -636,28 +636,32 @@ __device__ __forceinline__ void build_group(const Arena& A, int64_t g, int exclu
   }
   if (lane == 0) sh.run_off[n_rows] = total;
   __syncwarp();
-  // ---- the packed candidate stream, loads of the next chunk in flight ----
-  auto locate = [&](int c) -> int {  // sorted-atom index of candidate c (c < total)
-    int lo = 0, hi = n_rows - 1;  // last run with run_off <= c
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (sh.run_off[mid] <= c) lo = mid; else hi = mid - 1;
-    }
-    return sh.run_b[lo] + (c - sh.run_off[lo]);
+  // ---- the packed candidate stream, software-pipelined: while chunk c is
+  // tested, the position of chunk c+1 and the atom index of chunk c+2 are
+  // in flight.  Each lane walks the runs forward (candidate c is in run r
+  // when run_off[r] <= c < run_off[r+1]; chunks advance by 32, so the walk
+  // moves a step or two per chunk). ----
+  int run = 0;
+  auto locate = [&](int cc) -> int {  // sorted-atom index of candidate cc (cc < total), cc non-decreasing
+    while (sh.run_off[run + 1] <= cc) ++run;
+    return sh.run_b[run] + (cc - sh.run_off[run]);
   };
   int cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   unsigned ovf = 0u;
   const unsigned lt = (1u << lane) - 1u;
   int c = lane;
   int j = c < total ? A.cell_atoms[ab + locate(c)] : -1;
+  int j1 = c + 32 < total ? A.cell_atoms[ab + locate(c + 32)] : -1;
+  float4 pj = j >= 0 ? A.pos[j] : make_float4(0.f, 0.f, 0.f, 0.f);
   for (int c0 = 0; c0 < total; c0 += 32) {
     const bool valid = c < total;
-    const float4 pj = valid ? A.pos[j] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const int cn = c + 32;
-    const int jn = cn < total ? A.cell_atoms[ab + locate(cn)] : -1;
+    const float4 p1 = j1 >= 0 ? A.pos[j1] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const int j2 = c + 64 < total ? A.cell_atoms[ab + locate(c + 64)] : -1;
     group_test(A, sh, P, n_act, a0, (int)g, valid, j, pj, r2max, exclude_exc, lt, cnt, ovf);
-    c = cn;
-    j = jn;
+    c += 32;
+    j = j1;
+    pj = p1;
+    j1 = j2;
   }
   if (ovf) {
     if (lane == 0) atomicOr(&Sp->status, kStNbrOverflow);
