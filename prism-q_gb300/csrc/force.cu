@@ -543,29 +543,37 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_force(Arena A, int64_t n_sp
     // branch, so a lane keeps several gathers in flight and lanes never
     // diverge.  Pairs outside the cutoff contribute an exact zero, so the sum
     // is the same sequence of additions as a branching loop.
-    for (int t0 = 0; t0 < mine; t0 += 32) {
-      const int t1 = min(mine, t0 + 32);
-      int t = t0;
-      for (; t + 4 <= t1; t += 4) {
-        int j[4];
-        R4<R> pj[4];
-        R2<R> lj[4];
+    // The row indices of the next four entries are loaded while the current
+    // four are gathered and evaluated.  Partial sums flush after every 32 of
+    // the lane's entries, as in a loop over 32-entry chunks.
+    const int m4 = mine & ~3;
+    int jn[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) j[u] = __ldg(row + (int64_t)(t + u) * 32);
+    for (int u = 0; u < 4; ++u) jn[u] = m4 > 0 ? __ldg(row + (int64_t)u * 32) : 0;
+    for (int t = 0; t < m4; t += 4) {
+      int j[4];
+      R4<R> pj[4];
+      R2<R> lj[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          pj[u] = ldg_r4(pos + j[u]);
-          lj[u] = __ldg(ljp + j[u]);
-        }
+      for (int u = 0; u < 4; ++u) j[u] = jn[u];
+      if (t + 4 < m4) {
 #pragma unroll
-        for (int u = 0; u < 4; ++u) pair_accumulate<R>(pi, qi, li, pj[u], lj[u], cut2, f);
+        for (int u = 0; u < 4; ++u) jn[u] = __ldg(row + (int64_t)(t + 4 + u) * 32);
       }
-      for (; t < t1; ++t) {
-        const int j = __ldg(row + (int64_t)t * 32);
-        pair_accumulate<R>(pi, qi, li, ldg_r4(pos + j), __ldg(ljp + j), cut2, f);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        pj[u] = ldg_r4(pos + j[u]);
+        lj[u] = __ldg(ljp + j[u]);
       }
-      f.flush();
+#pragma unroll
+      for (int u = 0; u < 4; ++u) pair_accumulate<R>(pi, qi, li, pj[u], lj[u], cut2, f);
+      if (((t + 4) & 31) == 0) f.flush();
     }
+    for (int t = m4; t < mine; ++t) {
+      const int j = __ldg(row + (int64_t)t * 32);
+      pair_accumulate<R>(pi, qi, li, ldg_r4(pos + j), __ldg(ljp + j), cut2, f);
+    }
+    f.flush();
   } else
     for (int t0 = 0; t0 < mine; t0 += 32) {
       const int t1 = min(mine, t0 + 32);
