@@ -165,6 +165,49 @@ prismq_status prismq_polyala_build(int32_t n_chains, int32_t n_residues, uint64_
 prismq_status prismq_topology_view(const prismq_topology_buf* buf, prismq_topology* out);
 void prismq_topology_free(prismq_topology_buf* buf);
 
+/* ---- PRISM-PREP topology JSON (host only, no GPU) ----
+ *
+ * Replaces PrismPrepTopology::load (crates/prism-nhs/src/input.rs:1972),
+ * validate (:1996-2290), lower_harmonic_parameters (:467-520),
+ * validate_for_nonbonded_execution (:1429-1450) and apply_hmr (:2482-2560):
+ * the JSON a PRISM-PREP run writes becomes a prismq_topology ready for
+ * prismq_system_create / prismq_batch_add_system.
+ *   - Bond and angle force constants are lowered from the file's
+ *     harmonic_parameter_contract convention to U = k (x - x0)^2
+ *     (OPENMM_FULL_K_HALF_ENERGY: k x 0.5 in binary64, then float32).
+ *     The contract's canonical SHA-256 is checked.
+ *   - Strict exclusions come from `exclusions`; exact 1-4 pairs from
+ *     `nonbonded_exceptions`, whose completeness contract (counts and both
+ *     SHA-256 digests) is checked.
+ *   - Hydrogen mass repartitioning runs unless the file records
+ *     hmr_applied = true. */
+typedef struct prismq_prep_options {
+  int32_t apply_hmr;                 /* 1: repartition unless the file records it done (default 1) */
+  int32_t require_harmonic_contract; /* 1: refuse a file without harmonic_parameter_contract (default 1);
+                                        0: cast its coefficients to float32 unscaled */
+  int32_t require_exceptions;        /* 1: NonbondedExecutionPolicy::RequireExactV2 (default 1) */
+  int32_t reserved;
+  double hmr_factor;                 /* hydrogen mass multiplier (default 3.0) */
+} prismq_prep_options;
+
+typedef struct prismq_prep_report {
+  int32_t hmr_performed;             /* 1 if repartitioning ran during this load */
+  int32_t n_repartitioned;           /* clusters repartitioned */
+  int32_t n_skipped;                 /* clusters left alone (central atom would fall below 1 amu) */
+  int32_t exact_exceptions;          /* number of exact 1-4 exception pairs */
+  double bond_scale, angle_scale;    /* source / target energy prefactor applied to k */
+  double total_mass_before, total_mass_after;  /* cluster masses, amu (binary64) */
+} prismq_prep_report;
+
+void prismq_prep_options_default(prismq_prep_options* opt);
+/* Parse `len` bytes of UTF-8 JSON.  opt and report may be NULL (defaults; no report).
+ * PRISMQ_E_INVALID with prismq_last_error() naming the first violated rule. */
+prismq_status prismq_topology_from_prep_json(const char* text, size_t len, const prismq_prep_options* opt,
+                                             prismq_topology_buf** out, prismq_prep_report* report);
+/* Same, reading a file; PRISMQ_E_NOT_FOUND if it cannot be opened. */
+prismq_status prismq_topology_load_prep_json(const char* path, const prismq_prep_options* opt,
+                                             prismq_topology_buf** out, prismq_prep_report* report);
+
 /* ---- single system (the drop-in for NhsAmberFusedEngine, fused_engine.rs:6554) ---- */
 
 typedef struct prismq_system prismq_system;

@@ -12,6 +12,7 @@ calls fail loudly.
 from __future__ import annotations
 
 import ctypes
+import os
 import pathlib
 from dataclasses import dataclass
 
@@ -85,6 +86,18 @@ class ParamsStruct(ctypes.Structure):
                 ("constraint_check_fp64", ctypes.c_int32), ("precision", ctypes.c_int32)]
 
 
+class PrepOptionsStruct(ctypes.Structure):
+    _fields_ = [("apply_hmr", ctypes.c_int32), ("require_harmonic_contract", ctypes.c_int32),
+                ("require_exceptions", ctypes.c_int32), ("reserved", ctypes.c_int32), ("hmr_factor", ctypes.c_double)]
+
+
+class PrepReportStruct(ctypes.Structure):
+    _fields_ = [("hmr_performed", ctypes.c_int32), ("n_repartitioned", ctypes.c_int32),
+                ("n_skipped", ctypes.c_int32), ("exact_exceptions", ctypes.c_int32),
+                ("bond_scale", ctypes.c_double), ("angle_scale", ctypes.c_double),
+                ("total_mass_before", ctypes.c_double), ("total_mass_after", ctypes.c_double)]
+
+
 class ServerConfigStruct(ctypes.Structure):
     _fields_ = [("max_systems", ctypes.c_int32), ("chunk_steps", ctypes.c_int32), ("max_bypass_s", ctypes.c_double)]
 
@@ -136,6 +149,9 @@ def load() -> ctypes.CDLL:
         "prismq_polyala_build": (I, [ctypes.c_int32, ctypes.c_int32, ctypes.c_uint64, ctypes.c_float,
                                      ctypes.c_float, P]),
         "prismq_topology_view": (I, [P, P]),
+        "prismq_prep_options_default": (None, [P]),
+        "prismq_topology_from_prep_json": (I, [ctypes.c_char_p, ctypes.c_size_t, P, P, P]),
+        "prismq_topology_load_prep_json": (I, [ctypes.c_char_p, P, P, P]),
         "prismq_topology_free": (None, [P]),
         "prismq_system_create": (I, [P, P, P]),
         "prismq_system_destroy": (None, [P]),
@@ -290,6 +306,30 @@ class Topology:
         return t
 
     @classmethod
+    def _from_buf(cls, buf) -> "Topology":
+        """Copy the arrays of a prismq_topology_buf (the caller frees it)."""
+        L = load()
+        t = TopologyStruct()
+        _check(L.prismq_topology_view(buf, ctypes.byref(t)))
+        n = t.n_atoms
+
+        def arr(ptr, count, dtype, shape=None):
+            if count == 0:
+                return np.zeros(shape or 0, dtype=dtype)
+            nbytes = count * np.dtype(dtype).itemsize
+            raw = ctypes.string_at(ptr, nbytes)
+            a = np.frombuffer(raw, dtype=dtype).copy()
+            return a.reshape(shape) if shape else a
+
+        eoff = arr(t.exclusion_offsets, n + 1, np.int32)
+        return cls(arr(t.positions, 3 * n, np.float32, (n, 3)), arr(t.masses, n, np.float32),
+                   arr(t.charges, n, np.float32), arr(t.lj_sigma, n, np.float32),
+                   arr(t.lj_epsilon, n, np.float32), arr(t.bonds, t.n_bonds, BOND_DT),
+                   arr(t.angles, t.n_angles, ANGLE_DT), arr(t.dihedrals, t.n_dihedrals, DIH_DT),
+                   arr(t.exceptions, t.n_exceptions, EXC_DT), eoff,
+                   arr(t.exclusions, int(eoff[-1]), np.int32), arr(t.clusters, t.n_clusters, CLUSTER_DT))
+
+    @classmethod
     def polyala(cls, n_chains: int = 1, n_residues: int = 250, seed: int = 1, density: float = 0.03,
                 box_edge: float = 0.0) -> "Topology":
         """Seeded synthetic poly-alanine-like system (C generator in the library)."""
@@ -297,27 +337,43 @@ class Topology:
         buf = ctypes.c_void_p()
         _check(L.prismq_polyala_build(n_chains, n_residues, seed, density, box_edge, ctypes.byref(buf)))
         try:
-            t = TopologyStruct()
-            _check(L.prismq_topology_view(buf, ctypes.byref(t)))
-            n = t.n_atoms
-
-            def arr(ptr, count, dtype, shape=None):
-                if count == 0:
-                    return np.zeros(shape or 0, dtype=dtype)
-                nbytes = count * np.dtype(dtype).itemsize
-                raw = ctypes.string_at(ptr, nbytes)
-                a = np.frombuffer(raw, dtype=dtype).copy()
-                return a.reshape(shape) if shape else a
-
-            eoff = arr(t.exclusion_offsets, n + 1, np.int32)
-            return cls(arr(t.positions, 3 * n, np.float32, (n, 3)), arr(t.masses, n, np.float32),
-                       arr(t.charges, n, np.float32), arr(t.lj_sigma, n, np.float32),
-                       arr(t.lj_epsilon, n, np.float32), arr(t.bonds, t.n_bonds, BOND_DT),
-                       arr(t.angles, t.n_angles, ANGLE_DT), arr(t.dihedrals, t.n_dihedrals, DIH_DT),
-                       arr(t.exceptions, t.n_exceptions, EXC_DT), eoff,
-                       arr(t.exclusions, int(eoff[-1]), np.int32), arr(t.clusters, t.n_clusters, CLUSTER_DT))
+            return cls._from_buf(buf)
         finally:
             L.prismq_topology_free(buf)
+
+    @classmethod
+    def from_prep_json(cls, source, apply_hmr: bool = True, hmr_factor: float = 3.0,
+                       require_harmonic_contract: bool = True, require_exceptions: bool = True,
+                       report: dict | None = None) -> "Topology":
+        """A PRISM-PREP topology JSON (PrismPrepTopology, input.rs:1027-1140) lowered for the engine.
+
+        `source` is a path or the JSON text (str / bytes).  Validation, harmonic
+        lowering and hydrogen mass repartitioning run in the library; a
+        violated rule raises PrismQError with the rule named.  When `report`
+        is a dict it receives what the load did (HMR, scales, mass totals)."""
+        L = load()
+        opt = PrepOptionsStruct()
+        L.prismq_prep_options_default(ctypes.byref(opt))
+        opt.apply_hmr, opt.hmr_factor = int(bool(apply_hmr)), float(hmr_factor)
+        opt.require_harmonic_contract = int(bool(require_harmonic_contract))
+        opt.require_exceptions = int(bool(require_exceptions))
+        rep = PrepReportStruct()
+        buf = ctypes.c_void_p()
+        is_text = isinstance(source, (bytes, bytearray)) or (isinstance(source, str) and source.lstrip().startswith("{"))
+        if is_text:
+            data = source.encode() if isinstance(source, str) else bytes(source)
+            _check(L.prismq_topology_from_prep_json(data, len(data), ctypes.byref(opt), ctypes.byref(buf),
+                                                    ctypes.byref(rep)))
+        else:
+            _check(L.prismq_topology_load_prep_json(os.fsencode(source), ctypes.byref(opt), ctypes.byref(buf),
+                                                    ctypes.byref(rep)))
+        try:
+            topo = cls._from_buf(buf)
+        finally:
+            L.prismq_topology_free(buf)
+        if report is not None:
+            report.update({f: getattr(rep, f) for f, _ in PrepReportStruct._fields_})
+        return topo
 
     @classmethod
     def point_cloud(cls, positions) -> "Topology":

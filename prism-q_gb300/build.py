@@ -33,6 +33,7 @@ UNITS = {
     "noalloc.cu": ["--fmad=false"],
     "topology.cpp": [],
     "server.cpp": [],
+    "prep_json.cpp": [],
 }
 
 
