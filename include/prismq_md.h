@@ -235,6 +235,44 @@ prismq_status prismq_get_velocities(prismq_system* sys, float* vxyz);
 prismq_status prismq_get_step(prismq_system* sys, int64_t* step);
 prismq_status prismq_set_step(prismq_system* sys, int64_t step);
 
+/* ---- run protocol: per-step temperature, friction and timestep ----
+ *
+ * Replaces ProtocolState (protocol_state.cuh:14-62), its constructor
+ * ProtocolState::from_cryo_uv (protocol_state.rs:602-700), the director's
+ * per-step evaluation (protocol_director.cu:54-143) and
+ * NhsAmberFusedEngine::set_cryo_uv_protocol (fused_engine.rs:18815),
+ * compute_cryo_friction (:15366-15396) and set_adaptive_dt (:13986).
+ * The device evaluates the protocol at the start of every step inside the
+ * captured step graph (no extra launch); each system of a batch carries its
+ * own.  Step k after installation (k = 0, 1, ...) uses director step
+ * current_step + 1 + k.  UV bursts, wavelength scans and steering hints are
+ * not part of the MD step and are not carried. */
+typedef struct prismq_protocol {
+  float start_temp, end_temp;          /* K: cold and warm temperatures */
+  int32_t cold_hold_steps, ramp_steps, warm_hold_steps, ramp_down_steps, cold_return_steps;
+  float gamma_base;                    /* ps^-1 after equilibration */
+  int32_t cryo_enabled;                /* 1: γ x sqrt(300 / max(T, 10)) below 300 K */
+  int32_t equilibration_steps;         /* director steps of the friction blend (10000) */
+  float equilibration_gamma;           /* ps^-1 at the start of the blend (1000) */
+  int32_t adaptive_dt;                 /* 0: base_dt; 1: holds base_dt, ramps base_dt/2;
+                                          2: holds 1.5 base_dt, ramps base_dt */
+  float base_dt;                       /* ps */
+  int32_t current_step;                /* director step at installation (0) */
+} prismq_protocol;
+
+/* Physiological protocol: 300 K throughout, γ 1 ps^-1 after the reference's
+ * 10000-step equilibration blend from 1000 ps^-1, dt 0.004 ps, no cryo or
+ * adaptive dt. */
+void prismq_protocol_default(prismq_protocol* p);
+/* The protocol's values at one director step: out = {T (K), γ (ps^-1), dt (ps)}. */
+prismq_status prismq_protocol_eval(const prismq_protocol* p, int64_t director_step, float out[3]);
+/* Install a protocol (NULL removes it; the system keeps its current T, γ, dt).
+ * While one is installed, set_temperature / set_gamma return PRISMQ_E_INVALID
+ * and set_dt sets its base_dt. */
+prismq_status prismq_set_protocol(prismq_system* sys, const prismq_protocol* p);
+/* {T, γ, dt} the next step will use. */
+prismq_status prismq_get_step_params(prismq_system* sys, float out[3]);
+
 /* Force evaluation at the current positions (FORCE_N phase, nhs_amber_fused.cu:2993-3484).
  * pe_total: FP64 total potential energy (may be NULL).
  * f_aos: float[3N] kcal/mol/Å (may be NULL).  f_fixed: int64[3N] at 2^-32 (may be NULL). */
@@ -297,6 +335,9 @@ prismq_status prismq_batch_set_state(prismq_batch* b, int32_t slot, const float*
                                      const float* vxyz);
 prismq_status prismq_batch_get_step(prismq_batch* b, int32_t slot, int64_t* step);
 prismq_status prismq_batch_status(prismq_batch* b, int32_t slot);
+/* Run protocol of one resident system (see prismq_set_protocol). */
+prismq_status prismq_batch_set_protocol(prismq_batch* b, int32_t slot, const prismq_protocol* p);
+prismq_status prismq_batch_get_step_params(prismq_batch* b, int32_t slot, float out[3]);
 /* The autotuner's choice for the batch's force kernel: out[0] = variant
  * (-1 before the first step), out[1] = threads per block, out[2] = minimum
  * resident blocks per SM given to the register allocator.  The launch shape

@@ -68,6 +68,10 @@ def lib() -> ctypes.CDLL:
         L.orc_term_forces.argtypes = [P, P, P, P]
         L.orc_phases.argtypes = [P, ctypes.c_int, P, ctypes.c_longlong]
         L.orc_com_remove.argtypes = [P]
+        L.orc_protocol_eval.argtypes = [P, ctypes.c_longlong, P]
+        L.orc_protocol_eval.restype = None
+        L.orc_set_protocol.argtypes = [P, P, ctypes.c_longlong]
+        L.orc_set_protocol.restype = None
         L.orc_run.argtypes = [P, ctypes.c_long, ctypes.c_int]
         L.orc_step_count.restype = ctypes.c_longlong
         L.orc_step_count.argtypes = [P]
@@ -132,6 +136,14 @@ def pairs_brute(pos: np.ndarray, r2max: float = 144.0, excl_off=None, excl=None)
     return out[:n]
 
 
+def protocol_eval(proto_struct, director_step: int):
+    """(T, γ, dt, c1) of the oracle's director restatement; proto_struct is a
+    prismq_protocol (ctypes)."""
+    out = (ctypes.c_float * 4)()
+    lib().orc_protocol_eval(ctypes.byref(proto_struct), int(director_step), out)
+    return tuple(float(v) for v in out)
+
+
 def c1_of(gamma: float, dt: float) -> float:
     """exp(-γ·dt/2) rounded to float, computed as the library computes it."""
     hd = np.float32(0.5) * np.float32(dt)
@@ -160,6 +172,12 @@ class OracleSystem:
             self.close()
         except Exception:
             pass
+
+    def set_protocol(self, proto_struct, origin: int) -> None:
+        """Every step st then runs with the director's values at st - origin."""
+        self._proto = proto_struct
+        lib().orc_set_protocol(self.h, ctypes.byref(proto_struct) if proto_struct is not None else None,
+                               int(origin))
 
     def set_state(self, x=None, v=None):
         xa = None if x is None else np.ascontiguousarray(x, dtype=np.float32).reshape(-1)

@@ -328,6 +328,10 @@ struct orc_sys {
   /* REF27 rows cache */
   int* rows;
   int* rowlen;
+  /* run protocol: parameters of each step from the director restatement */
+  int proto_on;
+  prismq_protocol proto;
+  long long proto_origin; /* director step = step - proto_origin */
 };
 
 int orc_n_atoms(const orc_sys* s) { return s->n; }
@@ -1163,7 +1167,86 @@ void orc_term_forces(const orc_sys* s, float* fb, float* fa, float* fd) {
   }
 }
 
+/* ---- run protocol (protocol_director.cu:54-143, fused_engine.rs:15366-15396) ----
+ * e^x: x = k ln2 + r, |r| <= ln2/2, Taylor series of e^r to degree 17 by
+ * Horner's rule in binary64, times 2^k. */
+static double orc_exp(double x) {
+  if (x != x) return x;
+  if (x < -708.0) return 0.0;
+  if (x > 709.0) return HUGE_VAL;
+  const double ln2 = 0.69314718055994530941723212145818;
+  const double head = (double)(float)ln2, tail = ln2 - head;
+  const double kd = floor(x / ln2 + 0.5);
+  const double r = (x - kd * head) - kd * tail;
+  double fact = 1.0, coef[18];
+  for (int n = 0; n <= 17; ++n) {
+    if (n > 0) fact *= (double)n;
+    coef[n] = 1.0 / fact;
+  }
+  double p = coef[17];
+  for (int n = 16; n >= 0; --n) p = p * r + coef[n];
+  return ldexp(p, (int)kd);
+}
+
+void orc_protocol_eval(const prismq_protocol* P, long long director_step, float out[4]) {
+  const int s = director_step > 2147483647LL ? 2147483647 : (int)director_step;
+  const int e1 = P->cold_hold_steps, e2 = e1 + P->ramp_steps, e3 = e2 + P->warm_hold_steps,
+            e4 = e3 + P->ramp_down_steps;
+  float T;
+  int hold;
+  if (s < e1) {
+    T = P->start_temp;
+    hold = 1;
+  } else if (s < e2) {
+    const float prog = (float)(s - e1) / (float)(e2 - e1);
+    T = P->start_temp + prog * (P->end_temp - P->start_temp);
+    hold = 0;
+  } else if (s < e3) {
+    T = P->end_temp;
+    hold = 1;
+  } else if (s < e4) {
+    const float prog = (float)(s - e3) / (float)(e4 - e3);
+    T = P->end_temp - prog * (P->end_temp - P->start_temp);
+    hold = 0;
+  } else {
+    T = (P->ramp_down_steps == 0 && P->cold_return_steps == 0) ? P->end_temp : P->start_temp;
+    hold = 1;
+  }
+  float g = P->gamma_base;
+  if (s < P->equilibration_steps) {
+    const float prog = (float)s / (float)P->equilibration_steps;
+    const float decay = (float)orc_exp((double)(-3.0f * prog));
+    g = P->equilibration_gamma * decay + P->gamma_base * (1.0f - decay);
+  }
+  if (P->cryo_enabled && T < 300.0f) g = g * sqrtf(300.0f / (T > 10.0f ? T : 10.0f));
+  float dt = P->base_dt;
+  if (P->adaptive_dt == 2) dt = hold ? P->base_dt * 1.5f : P->base_dt;
+  if (P->adaptive_dt == 1) dt = hold ? P->base_dt : P->base_dt * 0.5f;
+  out[0] = T;
+  out[1] = g;
+  out[2] = dt;
+  out[3] = (float)orc_exp((double)(-g * (0.5f * dt)));
+}
+
+void orc_set_protocol(orc_sys* s, const prismq_protocol* p, long long origin) {
+  s->proto_on = p != NULL;
+  if (p) s->proto = *p;
+  s->proto_origin = origin;
+}
+
+/* The parameters of step `step` under the installed protocol. */
+static void protocol_step(orc_sys* s, long long step) {
+  if (!s->proto_on) return;
+  float o[4];
+  orc_protocol_eval(&s->proto, step - s->proto_origin, o);
+  s->p.temperature = o[0];
+  s->p.gamma = o[1];
+  s->p.dt = o[2];
+  s->p.c1 = o[3];
+}
+
 int orc_phases(orc_sys* s, int set, const int64_t* f_fixed, long long step) {
+  protocol_step(s, step);
   const int n = s->n;
   float* f = (float*)malloc(sizeof(float) * 3 * (size_t)n);
   for (int k = 0; k < 3 * n; ++k) f[k] = orc_fixed2f(f_fixed[k]);
@@ -1210,6 +1293,7 @@ int orc_run(orc_sys* s, long n_steps, int threads) {
   int err = 0;
   for (long it = 0; it < n_steps && !err; ++it) {
     const long long st = s->step;
+    protocol_step(s, st);
     if (s->p.com_interval > 0 && st > 0 && st % s->p.com_interval == 0) orc_com_remove(s);
     const int rebuild = (st == 0) || (st % 20 == 0);
     if ((err = forces_f32_impl(s, f, NULL, rebuild))) break;     /* FORCE_N */

@@ -81,6 +81,10 @@ void orc_term_forces(const orc_sys* s, float* fb, float* fa, float* fd);
  * SHAKE; set 2 = KICK½, RATTLE, OU½, clamp, RATTLE.  Returns 0 or an error
  * code (1 SHAKE, 2 RATTLE). */
 int orc_phases(orc_sys* s, int set, const int64_t* f_fixed, long long step);
+/* Run protocol: out = {T, gamma, dt, c1} at one director step; with a protocol
+ * installed every step st uses director step st - origin. */
+void orc_protocol_eval(const prismq_protocol* p, long long director_step, float out[4]);
+void orc_set_protocol(orc_sys* s, const prismq_protocol* p, long long origin);
 /* COM velocity removal (exact int64 Σ m·v, double Σ m). */
 void orc_com_remove(orc_sys* s);
 

@@ -86,6 +86,16 @@ class ParamsStruct(ctypes.Structure):
                 ("constraint_check_fp64", ctypes.c_int32), ("precision", ctypes.c_int32)]
 
 
+class ProtocolStruct(ctypes.Structure):
+    _fields_ = [("start_temp", ctypes.c_float), ("end_temp", ctypes.c_float),
+                ("cold_hold_steps", ctypes.c_int32), ("ramp_steps", ctypes.c_int32),
+                ("warm_hold_steps", ctypes.c_int32), ("ramp_down_steps", ctypes.c_int32),
+                ("cold_return_steps", ctypes.c_int32), ("gamma_base", ctypes.c_float),
+                ("cryo_enabled", ctypes.c_int32), ("equilibration_steps", ctypes.c_int32),
+                ("equilibration_gamma", ctypes.c_float), ("adaptive_dt", ctypes.c_int32),
+                ("base_dt", ctypes.c_float), ("current_step", ctypes.c_int32)]
+
+
 class PrepOptionsStruct(ctypes.Structure):
     _fields_ = [("apply_hmr", ctypes.c_int32), ("require_harmonic_contract", ctypes.c_int32),
                 ("require_exceptions", ctypes.c_int32), ("reserved", ctypes.c_int32), ("hmr_factor", ctypes.c_double)]
@@ -150,6 +160,12 @@ def load() -> ctypes.CDLL:
                                      ctypes.c_float, P]),
         "prismq_topology_view": (I, [P, P]),
         "prismq_prep_options_default": (None, [P]),
+        "prismq_protocol_default": (None, [P]),
+        "prismq_protocol_eval": (I, [P, i64, P]),
+        "prismq_set_protocol": (I, [P, P]),
+        "prismq_get_step_params": (I, [P, P]),
+        "prismq_batch_set_protocol": (I, [P, ctypes.c_int32, P]),
+        "prismq_batch_get_step_params": (I, [P, ctypes.c_int32, P]),
         "prismq_topology_from_prep_json": (I, [ctypes.c_char_p, ctypes.c_size_t, P, P, P]),
         "prismq_topology_load_prep_json": (I, [ctypes.c_char_p, P, P, P]),
         "prismq_topology_free": (None, [P]),
@@ -260,6 +276,41 @@ class Params:
                             self.rebuild_interval, self.com_interval, self.max_constraint_iter,
                             self.seed & 0xffffffff, self.stream & 0xffffffff, self.shake_tol, self.rattle_tol,
                             1 if self.constraint_check_fp64 else 0, int(self.precision))
+
+
+@dataclass
+class Protocol:
+    """Per-step temperature / friction / timestep schedule (ProtocolState,
+    protocol_state.cuh:14-62; director protocol_director.cu:54-143).  The
+    defaults are the physiological protocol with the reference's 10000-step
+    friction blend from 1000 ps^-1."""
+    start_temp: float = 300.0
+    end_temp: float = 300.0
+    cold_hold_steps: int = 0
+    ramp_steps: int = 0
+    warm_hold_steps: int = 100000
+    ramp_down_steps: int = 0
+    cold_return_steps: int = 0
+    gamma_base: float = 1.0
+    cryo_enabled: bool = False
+    equilibration_steps: int = 10000
+    equilibration_gamma: float = 1000.0
+    adaptive_dt: int = 0            # 1: ramps at base_dt/2; 2: holds at 1.5 base_dt
+    base_dt: float = 0.004
+    current_step: int = 0
+
+    def struct(self) -> ProtocolStruct:
+        return ProtocolStruct(self.start_temp, self.end_temp, self.cold_hold_steps, self.ramp_steps,
+                              self.warm_hold_steps, self.ramp_down_steps, self.cold_return_steps, self.gamma_base,
+                              1 if self.cryo_enabled else 0, self.equilibration_steps, self.equilibration_gamma,
+                              int(self.adaptive_dt), self.base_dt, self.current_step)
+
+    def eval(self, director_step: int) -> tuple[float, float, float]:
+        """(T, γ, dt) at one director step, computed by the library."""
+        out = (ctypes.c_float * 3)()
+        ps = self.struct()
+        _check(load().prismq_protocol_eval(ctypes.byref(ps), int(director_step), out))
+        return float(out[0]), float(out[1]), float(out[2])
 
 
 # ---------------------------------------------------------------- topology
@@ -428,6 +479,17 @@ class NhsAmberFusedEngine:
     def set_gamma(self, g: float) -> None:
         _check(load().prismq_set_gamma(self.h, g))
 
+    def set_protocol(self, protocol: "Protocol | None") -> None:
+        """Install a run protocol (set_cryo_uv_protocol, fused_engine.rs:18815); None removes it."""
+        ps = protocol.struct() if protocol is not None else None
+        _check(load().prismq_set_protocol(self.h, ctypes.byref(ps) if ps is not None else None))
+
+    def step_params(self) -> tuple[float, float, float]:
+        """(T, γ, dt) of the next step."""
+        out = (ctypes.c_float * 3)()
+        _check(load().prismq_get_step_params(self.h, out))
+        return float(out[0]), float(out[1]), float(out[2])
+
     def step(self, n_steps: int = 1) -> None:
         _check(load().prismq_step(self.h, n_steps))
 
@@ -565,6 +627,15 @@ class Batch:
 
     def status(self, slot: int) -> int:
         return load().prismq_batch_status(self.h, slot)
+
+    def set_protocol(self, slot: int, protocol: "Protocol | None") -> None:
+        ps = protocol.struct() if protocol is not None else None
+        _check(load().prismq_batch_set_protocol(self.h, slot, ctypes.byref(ps) if ps is not None else None))
+
+    def step_params(self, slot: int) -> tuple[float, float, float]:
+        out = (ctypes.c_float * 3)()
+        _check(load().prismq_batch_get_step_params(self.h, slot, out))
+        return float(out[0]), float(out[1]), float(out[2])
 
     def tuning(self) -> dict:
         """The autotuner's force-kernel launch shape for this batch."""

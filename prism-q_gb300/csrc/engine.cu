@@ -447,6 +447,74 @@ prismq_status check_params(const prismq_params* p) {
   return PRISMQ_OK;
 }
 
+// Host-side changes take effect from the next step as a whole: the
+// post-force phases still to run belong to that step too.
+void carry_post(SysDev* S) {
+  S->post_dt = S->dt;
+  S->post_temperature = S->temperature;
+  S->post_gamma = S->gamma;
+  S->post_c1 = S->c1;
+  S->post_c1d = S->c1d;
+}
+
+// With a protocol installed, the parameters of the next step (S->step) come
+// from the director, exactly as the control kernel evaluates them.
+void protocol_now(SysDev* S) {
+  if (!S->proto.on) return;
+  StepParams P;
+  protocol_eval(S->proto, S->step - S->proto.origin, &P);
+  S->dt = P.dt;
+  S->temperature = P.temperature;
+  S->gamma = P.gamma;
+  S->c1 = P.c1;
+  S->c1d = P.c1d;
+  carry_post(S);
+}
+
+prismq_status check_protocol(const prismq_protocol* p) {
+  if (!p) return fail(PRISMQ_E_INVALID, "protocol is NULL");
+  auto fin = [](float v) { return std::isfinite(v) && v >= 0.0f; };
+  if (!fin(p->start_temp) || !fin(p->end_temp)) return fail(PRISMQ_E_INVALID, "protocol temperatures must be >= 0");
+  if (!fin(p->gamma_base) || !fin(p->equilibration_gamma)) return fail(PRISMQ_E_INVALID, "protocol frictions must be >= 0");
+  if (!(p->base_dt > 0.0f) || !std::isfinite(p->base_dt)) return fail(PRISMQ_E_INVALID, "protocol base_dt must be positive");
+  const int64_t phases[5] = {p->cold_hold_steps, p->ramp_steps, p->warm_hold_steps, p->ramp_down_steps,
+                             p->cold_return_steps};
+  int64_t total = 0;
+  for (int64_t v : phases) {
+    if (v < 0) return fail(PRISMQ_E_INVALID, "protocol phase lengths must be >= 0");
+    total += v;
+  }
+  if (total > INT32_MAX) return fail(PRISMQ_E_INVALID, "protocol longer than 2^31-1 steps");
+  if (p->equilibration_steps < 0 || p->current_step < 0)
+    return fail(PRISMQ_E_INVALID, "protocol equilibration_steps and current_step must be >= 0");
+  if (p->adaptive_dt < 0 || p->adaptive_dt > 2) return fail(PRISMQ_E_INVALID, "protocol adaptive_dt must be 0, 1 or 2");
+  if (p->cryo_enabled != 0 && p->cryo_enabled != 1) return fail(PRISMQ_E_INVALID, "protocol cryo_enabled must be 0 or 1");
+  return PRISMQ_OK;
+}
+
+// ProtocolState::from_cryo_uv (protocol_state.rs:602-700): phase ends are
+// cumulative; the warm temperature persists when there is no cooling.
+ProtocolDev protocol_dev(const prismq_protocol& p, long long origin) {
+  ProtocolDev d;
+  std::memset(&d, 0, sizeof(d));
+  d.on = 1;
+  d.adaptive = p.adaptive_dt;
+  d.cryo = p.cryo_enabled;
+  d.warm_tail = (p.ramp_down_steps == 0 && p.cold_return_steps == 0) ? 1 : 0;
+  d.cold_hold_end = p.cold_hold_steps;
+  d.ramp_end = d.cold_hold_end + p.ramp_steps;
+  d.warm_hold_end = d.ramp_end + p.warm_hold_steps;
+  d.ramp_down_end = d.warm_hold_end + p.ramp_down_steps;
+  d.equil_steps = p.equilibration_steps;
+  d.start_temp = p.start_temp;
+  d.end_temp = p.end_temp;
+  d.gamma_base = p.gamma_base;
+  d.equil_gamma = p.equilibration_gamma;
+  d.base_dt = p.base_dt;
+  d.origin = origin;
+  return d;
+}
+
 void fill_params(SysDev* S, const prismq_params& p) {
   S->dt = p.dt;
   S->temperature = p.temperature;
@@ -468,6 +536,7 @@ void fill_params(SysDev* S, const prismq_params& p) {
   S->rattle_tol = p.rattle_tol > 0.f ? p.rattle_tol : 1.0e-5f;
   S->check64 = p.constraint_check_fp64;
   S->c1d = std::exp(-(double)p.gamma * 0.5 * (double)p.dt);
+  carry_post(S);
 }
 
 // ---------------------------------------------------------------------------
@@ -1556,9 +1625,17 @@ static prismq_status set_param_field(prismq_system* sys, int which, float v) {
   rc = B->sync_sys_from_device();
   if (rc != PRISMQ_OK) return rc;
   SysDev S = B->h_sys[sys->slot];
-  fill_params(&S, p);
+  if (S.proto.on) {
+    // a protocol owns T and γ; set_dt moves its base timestep (fused_engine.rs:15342)
+    if (which != 0) return fail(PRISMQ_E_INVALID, "a run protocol controls temperature and friction; remove it first");
+    S.proto.base_dt = v;
+    protocol_now(&S);
+  } else {
+    fill_params(&S, p);
+  }
   PQ_CK(cudaMemcpyAsync(B->A.sys + sys->slot, &S, sizeof(S), cudaMemcpyHostToDevice, B->st));
   PQ_CK(cudaStreamSynchronize(B->st));
+  B->h_sys[sys->slot] = S;
   B->slots[sys->slot].params = p;
   return PRISMQ_OK;
 }
@@ -1590,10 +1667,85 @@ prismq_status prismq_get_step(prismq_system* sys, int64_t* step) {
 prismq_status prismq_set_step(prismq_system* sys, int64_t step) {
   if (!sys || step < 0) return fail(PRISMQ_E_INVALID, "invalid argument");
   prismq_batch* B = sys->b;
-  const long long v = step;
-  PQ_CK(cudaMemcpyAsync(&B->A.sys[sys->slot].step, &v, sizeof(v), cudaMemcpyHostToDevice, B->st));
+  prismq_status rc = B->sync_sys_from_device();
+  if (rc != PRISMQ_OK) return rc;
+  SysDev S = B->h_sys[sys->slot];
+  S.step = step;
+  protocol_now(&S);  // the next step's parameters follow the counter
+  PQ_CK(cudaMemcpyAsync(B->A.sys + sys->slot, &S, sizeof(S), cudaMemcpyHostToDevice, B->st));
   PQ_CK(cudaStreamSynchronize(B->st));
+  B->h_sys[sys->slot] = S;
   return PRISMQ_OK;
+}
+
+void prismq_protocol_default(prismq_protocol* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->start_temp = 300.0f;
+  p->end_temp = 300.0f;
+  p->warm_hold_steps = 100000;  // TemperatureProtocol::physiological (fused_engine.rs:2996-3004)
+  p->gamma_base = 1.0f;
+  p->equilibration_steps = 10000;  // ProtocolState::from_cryo_uv (protocol_state.rs:676-677)
+  p->equilibration_gamma = 1000.0f;
+  p->base_dt = 0.004f;
+}
+
+prismq_status prismq_protocol_eval(const prismq_protocol* p, int64_t director_step, float out[3]) {
+  prismq_status rc = check_protocol(p);
+  if (rc != PRISMQ_OK) return rc;
+  if (!out) return fail(PRISMQ_E_INVALID, "out is NULL");
+  StepParams P;
+  protocol_eval(protocol_dev(*p, 0), director_step, &P);
+  out[0] = P.temperature;
+  out[1] = P.gamma;
+  out[2] = P.dt;
+  return PRISMQ_OK;
+}
+
+prismq_status prismq_batch_set_protocol(prismq_batch* b, int32_t slot, const prismq_protocol* p) {
+  prismq_status rc = check_slot(b, slot);
+  if (rc != PRISMQ_OK) return rc;
+  if (p && (rc = check_protocol(p)) != PRISMQ_OK) return rc;
+  if ((rc = b->sync_sys_from_device()) != PRISMQ_OK) return rc;
+  SysDev S = b->h_sys[slot];
+  if (p) {
+    // the next step is director step current_step + 1
+    S.proto = protocol_dev(*p, S.step - ((long long)p->current_step + 1));
+    protocol_now(&S);
+  } else {
+    S.proto.on = 0;
+    carry_post(&S);
+    prismq_params& q = b->slots[slot].params;
+    q.dt = S.dt;
+    q.temperature = S.temperature;
+    q.gamma = S.gamma;
+  }
+  PQ_CK(cudaMemcpyAsync(b->A.sys + slot, &S, sizeof(S), cudaMemcpyHostToDevice, b->st));
+  PQ_CK(cudaStreamSynchronize(b->st));
+  b->h_sys[slot] = S;
+  return PRISMQ_OK;
+}
+
+prismq_status prismq_batch_get_step_params(prismq_batch* b, int32_t slot, float out[3]) {
+  prismq_status rc = check_slot(b, slot);
+  if (rc != PRISMQ_OK) return rc;
+  if (!out) return fail(PRISMQ_E_INVALID, "out is NULL");
+  if ((rc = b->sync_sys_from_device()) != PRISMQ_OK) return rc;
+  const SysDev& S = b->h_sys[slot];
+  out[0] = S.temperature;
+  out[1] = S.gamma;
+  out[2] = S.dt;
+  return PRISMQ_OK;
+}
+
+prismq_status prismq_set_protocol(prismq_system* sys, const prismq_protocol* p) {
+  if (!sys) return fail(PRISMQ_E_INVALID, "system is NULL");
+  return prismq_batch_set_protocol(sys->b, sys->slot, p);
+}
+
+prismq_status prismq_get_step_params(prismq_system* sys, float out[3]) {
+  if (!sys) return fail(PRISMQ_E_INVALID, "system is NULL");
+  return prismq_batch_get_step_params(sys->b, sys->slot, out);
 }
 
 prismq_status prismq_step(prismq_system* sys, int64_t n_steps) {

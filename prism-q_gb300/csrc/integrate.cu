@@ -31,7 +31,15 @@ __global__ void __launch_bounds__(128, 8) k_integrate(Arena A, int64_t n_units, 
   int local[4];
   load_unit(A, U, u, local, S.atom_begin);
   int err = 0;
-  if ((mode & kIntPost) && s > 0) err = phases_post<R, kCheck64, true>(u, U, S, local, (uint64_t)(s - 1), A.noise);
+  if ((mode & kIntPost) && s > 0) {
+    SysDev SP = S;  // the post-force phases run with their own step's parameters
+    SP.dt = S.post_dt;
+    SP.temperature = S.post_temperature;
+    SP.gamma = S.post_gamma;
+    SP.c1 = S.post_c1;
+    SP.c1d = S.post_c1d;
+    err = phases_post<R, kCheck64, true>(u, U, SP, local, (uint64_t)(s - 1), A.noise);
+  }
   // On a COM step the pre-phase waits for the per-system COM reduction,
   // which runs in the control kernel.
   const bool pre = (mode & kIntPre) && !com_step;
@@ -57,16 +65,16 @@ __global__ void __launch_bounds__(256) k_noise(Arena A, int64_t n_atoms, int mod
   const int sid = A.atom_sys[a];
   if (sid < 0) return;
   const SysDev& S = A.sys[sid];
-  if (!S.active || S.status != 0 || S.gamma == 0.0f) return;
+  if (!S.active || S.status != 0) return;
   const long long s = S.step;
   const uint32_t local = (uint32_t)(a - S.atom_begin);
   float z0, z1, z2;
-  if ((mode & kIntPost) && s > 0) {
+  if ((mode & kIntPost) && s > 0 && S.post_gamma != 0.0f) {
     normal3(S.seed, S.stream, local, (uint64_t)(s - 1), kPurposeOuNp1, &z0, &z1, &z2);
     A.noise[a] = make_float4(z0, z1, z2, 0.0f);
   }
   const bool com_step = S.com_interval > 0 && s > 0 && (s % S.com_interval) == 0;
-  if ((mode & kIntPre) && !com_step) {
+  if ((mode & kIntPre) && !com_step && S.gamma != 0.0f) {
     normal3(S.seed, S.stream, local, (uint64_t)s, kPurposeOuN, &z0, &z1, &z2);
     A.noise[A.atom_cap + a] = make_float4(z0, z1, z2, 0.0f);
   }

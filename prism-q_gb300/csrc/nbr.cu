@@ -183,6 +183,24 @@ __global__ void __launch_bounds__(kCtlThreads) k_control_cells(Arena A, int mode
     } else {
       rb = !Sp->built || disp || Sp->steps_since_rebuild >= Sp->rebuild_interval;
       Sp->step = Sp->step + 1;
+      // This launch's integrate runs the post-force phases of the step just
+      // begun and the pre-force phases of the next one: keep this step's
+      // parameters for the former and, under a protocol, evaluate the
+      // director for the latter (protocol_director.cu:54-143).
+      Sp->post_dt = Sp->dt;
+      Sp->post_temperature = Sp->temperature;
+      Sp->post_gamma = Sp->gamma;
+      Sp->post_c1 = Sp->c1;
+      Sp->post_c1d = Sp->c1d;
+      if (Sp->proto.on) {
+        StepParams P;
+        protocol_eval(Sp->proto, Sp->step - Sp->proto.origin, &P);
+        Sp->dt = P.dt;
+        Sp->temperature = P.temperature;
+        Sp->gamma = P.gamma;
+        Sp->c1 = P.c1;
+        Sp->c1d = P.c1d;
+      }
     }
     if (atomicAdd(&Sp->status, 0) != 0) rb = false;
     // A prime pass (another system was admitted or reset) leaves the schedule

@@ -10,6 +10,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "pq_protocol.h"
+
 namespace pq {
 
 constexpr int kNbrCap = 1024;     // neighbour row capacity per atom
@@ -109,6 +111,13 @@ struct SysDev {
   int check64;  // 1: constraint residuals and multipliers evaluated in FP64
   int pad2;
   double c1d;   // exp(-γ·dt/2) in double (FP64 batches)
+  // The fields above (dt, temperature, gamma, c1, c1d) are the parameters of
+  // the step whose pre-force phases run next.  The post-force phases of a
+  // step run in the next launch, so the control kernel carries that step's
+  // values forward here before it moves the current set to the next step.
+  float post_dt, post_temperature, post_gamma, post_c1;
+  double post_c1d;
+  ProtocolDev proto;  // proto.on: the control kernel evaluates T, γ, dt every step
 };
 
 // Per-atom incidence into bonded term arrays (reference: atom_bond_list etc.,
