@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define PRISMQ_ABI_VERSION 2
+#define PRISMQ_ABI_VERSION 3
 
 typedef enum prismq_status {
   PRISMQ_OK = 0,
@@ -273,6 +273,36 @@ prismq_status prismq_set_protocol(prismq_system* sys, const prismq_protocol* p);
 /* {T, γ, dt} the next step will use. */
 prismq_status prismq_get_step_params(prismq_system* sys, float out[3]);
 
+/* ---- checkpoints: the dynamic state of one system at a step boundary ----
+ *
+ * Replaces the MD part of capture_process_checkpoint_fields /
+ * restore (fused_engine.rs:24718-25772): positions, velocities, the step
+ * counter, the neighbour-list schedule (steps since the last build, the
+ * positions of that build), the run parameters and the protocol.  A restored
+ * system continues bit for bit as the saved one would have: noise is
+ * counter-based, and rows rebuilt from the saved list-build positions give
+ * the same forces.  The blob is self-describing (magic, version, a topology
+ * fingerprint and a payload checksum); restore refuses a blob of another
+ * topology, size or library version, and a damaged one.  FP32 systems. */
+prismq_status prismq_checkpoint_size(prismq_system* sys, size_t* bytes);
+prismq_status prismq_checkpoint_save(prismq_system* sys, void* buf, size_t cap, size_t* written);
+prismq_status prismq_checkpoint_restore(prismq_system* sys, const void* buf, size_t len);
+
+/* ---- trajectory frames (the reference records none: D-FRAMES-NOT-CAPTURED) ----
+ *
+ * Every `interval` steps the step graph writes the state at that step
+ * boundary (positions after the step's drift and SHAKE, velocities after its
+ * post-force phases; the values prismq_get_positions / get_velocities return
+ * there) into a device ring of `capacity` frames, with no extra launch.
+ * interval 0 stops recording and frees the ring.  prismq_frames_read copies
+ * out, oldest first, up to max_frames frames not yet read: AoS float[3N] per
+ * frame into xyz (and vxyz when velocities were requested; may be NULL), the
+ * boundary step of each into steps (may be NULL).  *dropped counts frames
+ * overwritten before they were read.  FP32 systems. */
+prismq_status prismq_frames_configure(prismq_system* sys, int32_t interval, int32_t capacity, int32_t with_velocities);
+prismq_status prismq_frames_read(prismq_system* sys, float* xyz, float* vxyz, int64_t* steps, int32_t max_frames,
+                                 int32_t* n_out, int64_t* dropped);
+
 /* Force evaluation at the current positions (FORCE_N phase, nhs_amber_fused.cu:2993-3484).
  * pe_total: FP64 total potential energy (may be NULL).
  * f_aos: float[3N] kcal/mol/Å (may be NULL).  f_fixed: int64[3N] at 2^-32 (may be NULL). */
@@ -338,6 +368,17 @@ prismq_status prismq_batch_status(prismq_batch* b, int32_t slot);
 /* Run protocol of one resident system (see prismq_set_protocol). */
 prismq_status prismq_batch_set_protocol(prismq_batch* b, int32_t slot, const prismq_protocol* p);
 prismq_status prismq_batch_get_step_params(prismq_batch* b, int32_t slot, float out[3]);
+/* Checkpoint of one resident system (see prismq_checkpoint_save); a blob
+ * saved from a single system restores into a batch slot holding the same
+ * topology, and the other way round. */
+prismq_status prismq_batch_checkpoint_size(prismq_batch* b, int32_t slot, size_t* bytes);
+prismq_status prismq_batch_checkpoint_save(prismq_batch* b, int32_t slot, void* buf, size_t cap, size_t* written);
+prismq_status prismq_batch_checkpoint_restore(prismq_batch* b, int32_t slot, const void* buf, size_t len);
+/* Trajectory frames of one resident system (see prismq_frames_configure). */
+prismq_status prismq_batch_frames_configure(prismq_batch* b, int32_t slot, int32_t interval, int32_t capacity,
+                                            int32_t with_velocities);
+prismq_status prismq_batch_frames_read(prismq_batch* b, int32_t slot, float* xyz, float* vxyz, int64_t* steps,
+                                       int32_t max_frames, int32_t* n_out, int64_t* dropped);
 /* The autotuner's choice for the batch's force kernel: out[0] = variant
  * (-1 before the first step), out[1] = threads per block, out[2] = minimum
  * resident blocks per SM given to the register allocator.  The launch shape
@@ -400,6 +441,7 @@ typedef struct prismq_job {
   float* positions_out;            /* host float[3N] or NULL: final positions */
   float* velocities_out;           /* host float[3N] or NULL: final velocities */
   uint64_t tag;                    /* echoed in the result */
+  const struct prismq_protocol* protocol; /* NULL: constant T, γ, dt; else copied by submit */
 } prismq_job;
 
 typedef struct prismq_job_result {

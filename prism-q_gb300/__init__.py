@@ -114,7 +114,7 @@ class ServerConfigStruct(ctypes.Structure):
 
 class JobStruct(ctypes.Structure):
     _fields_ = [("topology", _P), ("params", ParamsStruct), ("n_steps", ctypes.c_int64),
-                ("positions_out", _P), ("velocities_out", _P), ("tag", ctypes.c_uint64)]
+                ("positions_out", _P), ("velocities_out", _P), ("tag", ctypes.c_uint64), ("protocol", _P)]
 
 
 class JobResultStruct(ctypes.Structure):
@@ -166,6 +166,16 @@ def load() -> ctypes.CDLL:
         "prismq_get_step_params": (I, [P, P]),
         "prismq_batch_set_protocol": (I, [P, ctypes.c_int32, P]),
         "prismq_batch_get_step_params": (I, [P, ctypes.c_int32, P]),
+        "prismq_checkpoint_size": (I, [P, P]),
+        "prismq_checkpoint_save": (I, [P, P, ctypes.c_size_t, P]),
+        "prismq_checkpoint_restore": (I, [P, P, ctypes.c_size_t]),
+        "prismq_batch_checkpoint_size": (I, [P, ctypes.c_int32, P]),
+        "prismq_batch_checkpoint_save": (I, [P, ctypes.c_int32, P, ctypes.c_size_t, P]),
+        "prismq_batch_checkpoint_restore": (I, [P, ctypes.c_int32, P, ctypes.c_size_t]),
+        "prismq_frames_configure": (I, [P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
+        "prismq_frames_read": (I, [P, P, P, P, ctypes.c_int32, P, P]),
+        "prismq_batch_frames_configure": (I, [P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
+        "prismq_batch_frames_read": (I, [P, ctypes.c_int32, P, P, P, ctypes.c_int32, P, P]),
         "prismq_topology_from_prep_json": (I, [ctypes.c_char_p, ctypes.c_size_t, P, P, P]),
         "prismq_topology_load_prep_json": (I, [ctypes.c_char_p, P, P, P]),
         "prismq_topology_free": (None, [P]),
@@ -435,6 +445,28 @@ class Topology:
                    np.full(n, 0.1, np.float32))
 
 
+def _read_frames(call, n_atoms: int, velocities: bool, max_frames: int, chunk: int = 64) -> dict:
+    xs, vs, steps, dropped = [], [], [], 0
+    while len(steps) < max_frames:
+        want = min(chunk, max_frames - len(steps))
+        x = np.zeros((want, n_atoms, 3), np.float32)
+        v = np.zeros((want, n_atoms, 3), np.float32) if velocities else None
+        st = np.zeros(want, np.int64)
+        got, lost = ctypes.c_int32(), ctypes.c_int64()
+        _check(call(_ptr(x), _ptr(v) if v is not None else None, _ptr(st), want, ctypes.byref(got),
+                    ctypes.byref(lost)))
+        dropped += lost.value
+        k = got.value
+        xs.append(x[:k])
+        if v is not None:
+            vs.append(v[:k])
+        steps.extend(st[:k].tolist())
+        if k < want:
+            break
+    return {"steps": np.array(steps, np.int64), "positions": np.concatenate(xs) if xs else np.zeros((0, n_atoms, 3)),
+            "velocities": (np.concatenate(vs) if vs else None), "dropped": dropped}
+
+
 # ---------------------------------------------------------------- engine
 class NhsAmberFusedEngine:
     """One system on the GPU (the drop-in for the reference engine's MD step)."""
@@ -489,6 +521,34 @@ class NhsAmberFusedEngine:
         out = (ctypes.c_float * 3)()
         _check(load().prismq_get_step_params(self.h, out))
         return float(out[0]), float(out[1]), float(out[2])
+
+    def checkpoint(self) -> bytes:
+        """The system's dynamic state at this step boundary (restore() resumes it bit for bit)."""
+        L = load()
+        n = ctypes.c_size_t()
+        _check(L.prismq_checkpoint_size(self.h, ctypes.byref(n)))
+        buf = ctypes.create_string_buffer(n.value)
+        _check(L.prismq_checkpoint_save(self.h, buf, n.value, None))
+        return buf.raw
+
+    def restore(self, blob: bytes) -> None:
+        _check(load().prismq_checkpoint_restore(self.h, blob, len(blob)))
+
+    def record_frames(self, interval: int, capacity: int = 64, velocities: bool = False) -> None:
+        """Record the state every `interval` steps into a device ring of `capacity` frames (0 stops)."""
+        _check(load().prismq_frames_configure(self.h, interval, capacity, 1 if velocities else 0))
+        self._frame_vel = velocities
+
+    def read_frames(self, max_frames: int = 1 << 30):
+        """Frames not yet read, oldest first: dict(steps, positions [F,N,3], velocities or None, dropped)."""
+        return _read_frames(lambda *a: load().prismq_frames_read(self.h, *a), self.n_atoms,
+                            getattr(self, "_frame_vel", False), max_frames)
+
+    def save_checkpoint(self, path) -> None:
+        pathlib.Path(path).write_bytes(self.checkpoint())
+
+    def load_checkpoint(self, path) -> None:
+        self.restore(pathlib.Path(path).read_bytes())
 
     def step(self, n_steps: int = 1) -> None:
         _check(load().prismq_step(self.h, n_steps))
@@ -637,6 +697,26 @@ class Batch:
         _check(load().prismq_batch_get_step_params(self.h, slot, out))
         return float(out[0]), float(out[1]), float(out[2])
 
+    def checkpoint(self, slot: int) -> bytes:
+        L = load()
+        n = ctypes.c_size_t()
+        _check(L.prismq_batch_checkpoint_size(self.h, slot, ctypes.byref(n)))
+        buf = ctypes.create_string_buffer(n.value)
+        _check(L.prismq_batch_checkpoint_save(self.h, slot, buf, n.value, None))
+        return buf.raw
+
+    def restore(self, slot: int, blob: bytes) -> None:
+        _check(load().prismq_batch_checkpoint_restore(self.h, slot, blob, len(blob)))
+
+    def record_frames(self, slot: int, interval: int, capacity: int = 64, velocities: bool = False) -> None:
+        _check(load().prismq_batch_frames_configure(self.h, slot, interval, capacity, 1 if velocities else 0))
+        self._frame_cfg = getattr(self, "_frame_cfg", {})
+        self._frame_cfg[slot] = velocities
+
+    def read_frames(self, slot: int, n_atoms: int, max_frames: int = 1 << 30):
+        vel = getattr(self, "_frame_cfg", {}).get(slot, False)
+        return _read_frames(lambda *a: load().prismq_batch_frames_read(self.h, slot, *a), n_atoms, vel, max_frames)
+
     def tuning(self) -> dict:
         """The autotuner's force-kernel launch shape for this batch."""
         out = np.zeros(3, np.int32)
@@ -737,13 +817,15 @@ class Server:
         self.close()
 
     def submit(self, topology: Topology, n_steps: int, params: Params | None = None, tag: int = 0,
-               want_state: bool = True) -> int:
+               want_state: bool = True, protocol: "Protocol | None" = None) -> int:
         n = topology.n_atoms
         x = np.zeros((n, 3), np.float32) if want_state else None
         v = np.zeros((n, 3), np.float32) if want_state else None
         t = topology.struct()
+        ps = protocol.struct() if protocol is not None else None
         job = JobStruct(ctypes.cast(ctypes.pointer(t), _P), (params or Params()).struct(), int(n_steps),
-                        _ptr(x), _ptr(v), int(tag) & 0xffffffffffffffff)
+                        _ptr(x), _ptr(v), int(tag) & 0xffffffffffffffff,
+                        ctypes.cast(ctypes.pointer(ps), _P) if ps is not None else None)
         jid = ctypes.c_int64()
         _check(load().prismq_server_submit(self.h, ctypes.byref(job), ctypes.byref(jid)))
         self._out[jid.value] = (x, v)  # the worker writes here when the job ends

@@ -131,9 +131,48 @@ struct Lowered {
   int ref_dims[3] = {1, 1, 1};
   bool ref_ok = false;
   int cell_cap = 64;
+  uint64_t topo_hash = 0;  // fingerprint of everything but positions and velocities
 };
 
 bool finite_pos(float x) { return std::isfinite(x); }
+
+// 64-bit FNV-1a over 8-byte words (then the tail bytes): a fingerprint that
+// tells a checkpoint which topology it belongs to.
+uint64_t fnv_words(uint64_t h, const void* data, size_t n) {
+  const unsigned char* b = static_cast<const unsigned char*>(data);
+  size_t i = 0;
+  for (; i + 8 <= n; i += 8) {
+    uint64_t w;
+    std::memcpy(&w, b + i, 8);
+    h = (h ^ w) * 1099511628211ull;
+  }
+  for (; i < n; ++i) h = (h ^ b[i]) * 1099511628211ull;
+  return h;
+}
+template <class T>
+uint64_t fnv_vec(uint64_t h, const std::vector<T>& v) {
+  const uint64_t n = v.size();
+  h = fnv_words(h, &n, sizeof(n));
+  return v.empty() ? h : fnv_words(h, v.data(), sizeof(T) * v.size());
+}
+
+uint64_t topology_fingerprint(const Lowered& L) {
+  uint64_t h = 14695981039346656037ull;
+  h = fnv_words(h, &L.n, sizeof(L.n));
+  h = fnv_vec(h, L.charges);
+  h = fnv_vec(h, L.masses);
+  h = fnv_vec(h, L.lj);
+  h = fnv_vec(h, L.mask_all);
+  h = fnv_vec(h, L.mask_ref);
+  h = fnv_vec(h, L.far);
+  h = fnv_vec(h, L.far_list);
+  h = fnv_vec(h, L.bonds);
+  h = fnv_vec(h, L.angles);
+  h = fnv_vec(h, L.dihs);
+  h = fnv_vec(h, L.excs);
+  h = fnv_vec(h, L.units);
+  return h;
+}
 
 prismq_status lower_topology(const prismq_topology* T, Lowered* L) {
   if (!T) return fail(PRISMQ_E_INVALID, "topology is NULL");
@@ -400,6 +439,7 @@ prismq_status lower_topology(const prismq_topology* T, Lowered* L) {
     ref_cells *= L->ref_dims[d];
   }
   L->cell_cap = (int)std::max<long long>({1024LL, (long long)n / 2, L->ref_ok ? ref_cells : 0LL});
+  L->topo_hash = topology_fingerprint(*L);
   return PRISMQ_OK;
 }
 
@@ -636,6 +676,13 @@ struct SlotRec {
   bool ref_ok = false;
   bool need_prime = true;
   prismq_params params{};
+  uint64_t topo_hash = 0;
+  // trajectory-frame ring (device memory outside the arena): frame i of the
+  // ring holds positions [n_atoms] then, with velocities, [n_atoms] more
+  float4* fr_mem = nullptr;
+  int fr_interval = 0, fr_cap = 0, fr_vel = 0;
+  int64_t fr_written = 0, fr_read = 0;  // frames recorded / handed out so far
+  std::vector<int64_t> fr_steps;        // boundary step of each ring entry
 };
 
 }  // namespace
@@ -661,6 +708,8 @@ struct prismq_batch {
   std::vector<SysDev> h_sys;
 
   ~prismq_batch() {
+    for (auto& r : slots)
+      if (r.fr_mem) cudaFree(r.fr_mem);
     if (gexec) cudaGraphExecDestroy(gexec);
     void* ptrs[] = {A.pos, A.vel, A.lj, A.xref, A.f, A.pe, A.atom_sys, A.mask_all, A.mask_ref, A.far,
                     A.far_list, A.inc, A.inc_list, A.ex_idx, A.ex_partner, A.ex_par, A.exc, A.grp, A.grp_refs, A.bonds, A.angles,
@@ -873,9 +922,55 @@ struct prismq_batch {
     return check_status();
   }
 
+  // Steps in segments that end on every trajectory-frame boundary of the
+  // resident systems; after each segment the systems at a boundary copy their
+  // state into their rings.  A segment ends with the post-force phases, which
+  // is where any call of step() ends, so results do not depend on the frames.
+  prismq_status step_with_frames(int64_t n) {
+    prismq_status rc = sync_sys_from_device();
+    if (rc != PRISMQ_OK) return rc;
+    prismq_status first_failure = PRISMQ_OK;  // a failed system freezes; the others run on
+    while (n > 0) {
+      int64_t m = n;
+      for (int i = 0; i < sys_span; ++i) {
+        const SlotRec& R = slots[i];
+        if (!R.active || R.fr_interval <= 0 || h_sys[i].status != 0) continue;
+        m = std::min<int64_t>(m, R.fr_interval - h_sys[i].step % R.fr_interval);
+      }
+      rc = step_segment(m);
+      if (rc == PRISMQ_E_SHAKE || rc == PRISMQ_E_RATTLE || rc == PRISMQ_E_NONFINITE || rc == PRISMQ_E_CELL_OVERFLOW ||
+          rc == PRISMQ_E_NEIGHBOR_OVERFLOW) {
+        if (first_failure == PRISMQ_OK) first_failure = rc;
+      } else if (rc != PRISMQ_OK) {
+        return rc;
+      }
+      for (int i = 0; i < sys_span; ++i) {  // h_sys was refreshed by the status check
+        SlotRec& R = slots[i];
+        const SysDev& S = h_sys[i];
+        if (!R.active || R.fr_interval <= 0 || S.status != 0 || S.step % R.fr_interval != 0) continue;
+        if (R.fr_written > 0 && R.fr_steps[(R.fr_written - 1) % R.fr_cap] == S.step) continue;
+        const int64_t slot = R.fr_written % R.fr_cap;
+        const size_t plane = sizeof(float4) * (size_t)R.n_atoms;
+        float4* dst = R.fr_mem + slot * (R.fr_vel ? 2 : 1) * R.n_atoms;
+        PQ_CK(cudaMemcpyAsync(dst, A.pos + R.atom_b, plane, cudaMemcpyDeviceToDevice, st));
+        if (R.fr_vel) PQ_CK(cudaMemcpyAsync(dst + R.n_atoms, A.vel + R.atom_b, plane, cudaMemcpyDeviceToDevice, st));
+        R.fr_steps[slot] = S.step;
+        R.fr_written += 1;
+      }
+      n -= m;
+    }
+    return first_failure;
+  }
+
   prismq_status step(int64_t n) {
     if (n <= 0) return PRISMQ_OK;
     if (sys_span == 0) return PRISMQ_OK;
+    for (int i = 0; i < sys_span; ++i)
+      if (slots[i].active && slots[i].fr_interval > 0) return step_with_frames(n);
+    return step_segment(n);
+  }
+
+  prismq_status step_segment(int64_t n) {
     prismq_status rc = prime_if_needed();
     if (rc != PRISMQ_OK) return rc;
     rc = ensure_graph();
@@ -1182,6 +1277,7 @@ prismq_status batch_admit(prismq_batch* B, const Lowered& L0, const prismq_param
   R.ref_ok = L.ref_ok;
   R.need_prime = true;
   R.params = p;
+  R.topo_hash = L.topo_hash;
   B->slots[slot] = R;
   B->h_sys[slot] = S;
   B->update_spans();
@@ -1202,6 +1298,7 @@ prismq_status batch_release(prismq_batch* B, int slot) {
                         sizeof(int2) * ((R.n_atoms + kForceGroup - 1) / kForceGroup), st));
   PQ_CK(cudaMemsetAsync(A.sys + slot, 0, sizeof(SysDev), st));
   PQ_CK(cudaStreamSynchronize(st));
+  if (R.fr_mem) cudaFree(R.fr_mem);
   B->r_atoms.release(R.atom_b, R.n_atoms);
   B->r_units.release(R.unit_b, R.n_units);
   B->r_bonds.release(R.bond_b, R.n_bonds);
@@ -1871,6 +1968,255 @@ prismq_status prismq_debug_phases(prismq_system* sys, prismq_phase_set set, int6
   PQ_CK(cudaGetLastError());
   PQ_CK(cudaStreamSynchronize(B->st));
   return B->check_status(sys->slot);
+}
+
+// ---------------------------------------------------------------------------
+// Checkpoints: the complete dynamic state of one system at a step boundary.
+// A restored system continues bit for bit as if it had never stopped.  The
+// noise is counter-based (no generator state) and the forces are recomputed
+// from the saved positions over neighbour rows rebuilt from the saved
+// list-build positions, which reproduces the rows, their order and so the
+// forces exactly.
+// ---------------------------------------------------------------------------
+namespace {
+
+struct CkptHeader {
+  char magic[8];          // "PQCKPT" 0 1
+  uint32_t version;       // 1
+  uint32_t header_bytes;  // sizeof(CkptHeader)
+  int32_t n_atoms, precision;
+  uint64_t topo_hash;
+  int64_t step, n_rebuilds;
+  int32_t steps_since_rebuild, built, displaced, nbr_mode;
+  int32_t pending_prime, pad0;
+  prismq_params params;
+  float dt, temperature, gamma, c1;
+  double c1d;
+  ProtocolDev proto;
+  float ref_origin[3];
+  int32_t ref_dims[3];
+  uint64_t payload_bytes;
+  uint64_t payload_hash;  // x, v and list-build positions, float AoS
+};
+constexpr char kCkptMagic[8] = {'P', 'Q', 'C', 'K', 'P', 'T', 0, 1};
+
+size_t ckpt_bytes(int64_t n) { return sizeof(CkptHeader) + 3 * 3 * sizeof(float) * (size_t)n; }
+
+}  // namespace
+
+prismq_status prismq_batch_checkpoint_size(prismq_batch* b, int32_t slot, size_t* bytes) {
+  prismq_status rc = check_slot(b, slot);
+  if (rc != PRISMQ_OK) return rc;
+  if (!bytes) return fail(PRISMQ_E_INVALID, "bytes is NULL");
+  *bytes = ckpt_bytes(b->slots[slot].n_atoms);
+  return PRISMQ_OK;
+}
+
+prismq_status prismq_batch_checkpoint_save(prismq_batch* b, int32_t slot, void* buf, size_t cap, size_t* written) {
+  prismq_status rc = check_slot(b, slot);
+  if (rc != PRISMQ_OK) return rc;
+  if (!buf) return fail(PRISMQ_E_INVALID, "buffer is NULL");
+  if (b->A.fp64) return fail(PRISMQ_E_INVALID, "checkpoints cover FP32 systems");
+  const SlotRec& R = b->slots[slot];
+  const int64_t n = R.n_atoms;
+  if (cap < ckpt_bytes(n)) return fail(PRISMQ_E_CAPACITY, "checkpoint buffer too small");
+  if ((rc = b->check_status(slot)) != PRISMQ_OK) return rc;  // a failed system has no state to resume
+  const SysDev& S = b->h_sys[slot];
+  CkptHeader h;
+  std::memset(&h, 0, sizeof(h));
+  std::memcpy(h.magic, kCkptMagic, 8);
+  h.version = 1;
+  h.header_bytes = sizeof(CkptHeader);
+  h.n_atoms = (int32_t)n;
+  h.precision = PRISMQ_PRECISION_FP32;
+  h.topo_hash = R.topo_hash;
+  h.step = S.step;
+  h.n_rebuilds = S.n_rebuilds;
+  h.steps_since_rebuild = S.steps_since_rebuild;
+  h.built = S.built;
+  h.displaced = S.displaced;
+  h.nbr_mode = S.nbr_mode;
+  h.pending_prime = (R.need_prime || S.need_prime || !S.built) ? 1 : 0;
+  h.params = R.params;
+  h.dt = S.dt;
+  h.temperature = S.temperature;
+  h.gamma = S.gamma;
+  h.c1 = S.c1;
+  h.c1d = S.c1d;
+  h.proto = S.proto;
+  for (int d = 0; d < 3; ++d) {
+    h.ref_origin[d] = S.ref_origin[d];
+    h.ref_dims[d] = S.ref_dims[d];
+  }
+  h.payload_bytes = 9 * sizeof(float) * (size_t)n;
+  float* x = reinterpret_cast<float*>(static_cast<char*>(buf) + sizeof(CkptHeader));
+  if ((rc = get_xyz(b, slot, b->A.pos, x)) != PRISMQ_OK) return rc;
+  if ((rc = get_xyz(b, slot, b->A.vel, x + 3 * n)) != PRISMQ_OK) return rc;
+  if ((rc = get_xyz(b, slot, b->A.xref, x + 6 * n)) != PRISMQ_OK) return rc;
+  h.payload_hash = fnv_words(14695981039346656037ull, x, h.payload_bytes);
+  std::memcpy(buf, &h, sizeof(h));
+  if (written) *written = ckpt_bytes(n);
+  return PRISMQ_OK;
+}
+
+prismq_status prismq_batch_checkpoint_restore(prismq_batch* b, int32_t slot, const void* buf, size_t len) {
+  prismq_status rc = check_slot(b, slot);
+  if (rc != PRISMQ_OK) return rc;
+  if (!buf) return fail(PRISMQ_E_INVALID, "buffer is NULL");
+  if (b->A.fp64) return fail(PRISMQ_E_INVALID, "checkpoints cover FP32 systems");
+  SlotRec& R = b->slots[slot];
+  const int64_t n = R.n_atoms;
+  CkptHeader h;
+  if (len < sizeof(h)) return fail(PRISMQ_E_INVALID, "checkpoint truncated");
+  std::memcpy(&h, buf, sizeof(h));
+  if (std::memcmp(h.magic, kCkptMagic, 8) != 0 || h.version != 1 || h.header_bytes != sizeof(CkptHeader))
+    return fail(PRISMQ_E_INVALID, "not a checkpoint of this library version");
+  if (h.n_atoms != n || h.precision != PRISMQ_PRECISION_FP32)
+    return fail(PRISMQ_E_INVALID, "checkpoint is for a system of another size or precision");
+  if (h.topo_hash != R.topo_hash) return fail(PRISMQ_E_INVALID, "checkpoint belongs to another topology");
+  if (h.payload_bytes != 9 * sizeof(float) * (size_t)n || len != ckpt_bytes(n))
+    return fail(PRISMQ_E_INVALID, "checkpoint truncated or padded");
+  const float* x = reinterpret_cast<const float*>(static_cast<const char*>(buf) + sizeof(CkptHeader));
+  if (fnv_words(14695981039346656037ull, x, h.payload_bytes) != h.payload_hash)
+    return fail(PRISMQ_E_INVALID, "checkpoint payload is corrupted");
+  if ((rc = check_params(&h.params)) != PRISMQ_OK) return rc;
+  if (h.params.precision != PRISMQ_PRECISION_FP32) return fail(PRISMQ_E_INVALID, "checkpoint precision");
+  if (h.step < 0 || h.built < 0 || h.built > 1 || (h.nbr_mode != 0 && h.nbr_mode != 1))
+    return fail(PRISMQ_E_INVALID, "checkpoint control state out of range");
+  if ((rc = b->sync_sys_from_device()) != PRISMQ_OK) return rc;
+  SysDev S = b->h_sys[slot];
+  S.status = 0;
+  S.nbr_mode = h.nbr_mode;
+  for (int d = 0; d < 3; ++d) {
+    S.ref_origin[d] = h.ref_origin[d];
+    S.ref_dims[d] = h.ref_dims[d];
+  }
+  fill_params(&S, h.params);
+  if (!h.pending_prime) {
+    // rebuild the rows from the positions of the last list build, then
+    // evaluate the forces at the saved positions over them
+    if ((rc = set_xyz(b, slot, b->A.pos, x + 6 * n)) != PRISMQ_OK) return rc;
+    S.need_prime = 1;
+    S.built = 0;
+    PQ_CK(cudaMemcpyAsync(b->A.sys + slot, &S, sizeof(S), cudaMemcpyHostToDevice, b->st));
+    if ((rc = b->prime_flagged()) != PRISMQ_OK) return rc;
+    if ((rc = set_xyz(b, slot, b->A.pos, x)) != PRISMQ_OK) return rc;
+    launch_force(b->A, b->atom_span, false, b->st, true, 0, b->group_slots);
+    g_launches += 1;
+    PQ_CK(cudaGetLastError());
+    if ((rc = b->sync_sys_from_device()) != PRISMQ_OK) return rc;
+    S = b->h_sys[slot];
+    if (S.status != 0) return b->check_status(slot);
+  } else if ((rc = set_xyz(b, slot, b->A.pos, x)) != PRISMQ_OK) {
+    return rc;
+  }
+  if ((rc = set_xyz(b, slot, b->A.vel, x + 3 * n)) != PRISMQ_OK) return rc;
+  S.step = h.step;
+  S.n_rebuilds = h.n_rebuilds;
+  S.steps_since_rebuild = h.steps_since_rebuild;
+  S.built = h.built;
+  S.displaced = h.displaced;
+  S.need_prime = h.pending_prime;
+  S.dt = h.dt;
+  S.temperature = h.temperature;
+  S.gamma = h.gamma;
+  S.c1 = h.c1;
+  S.c1d = h.c1d;
+  carry_post(&S);
+  S.proto = h.proto;
+  PQ_CK(cudaMemcpyAsync(b->A.sys + slot, &S, sizeof(S), cudaMemcpyHostToDevice, b->st));
+  PQ_CK(cudaStreamSynchronize(b->st));
+  b->h_sys[slot] = S;
+  R.params = h.params;
+  R.need_prime = h.pending_prime != 0;
+  return PRISMQ_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Trajectory frames
+// ---------------------------------------------------------------------------
+prismq_status prismq_batch_frames_configure(prismq_batch* b, int32_t slot, int32_t interval, int32_t capacity,
+                                            int32_t with_velocities) {
+  prismq_status rc = check_slot(b, slot);
+  if (rc != PRISMQ_OK) return rc;
+  if (b->A.fp64) return fail(PRISMQ_E_INVALID, "trajectory frames cover FP32 systems");
+  if (interval < 0 || (interval > 0 && capacity < 1)) return fail(PRISMQ_E_INVALID, "interval >= 0, capacity >= 1");
+  SlotRec& R = b->slots[slot];
+  float4* mem = nullptr;
+  if (interval > 0) {
+    const size_t bytes = (size_t)capacity * (with_velocities ? 2 : 1) * sizeof(float4) * (size_t)R.n_atoms;
+    if (cudaMalloc(&mem, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(PRISMQ_E_CAPACITY, "no device memory for " + std::to_string(capacity) + " frames");
+    }
+  }
+  PQ_CK(cudaStreamSynchronize(b->st));  // no copy into the old ring is still in flight
+  if (R.fr_mem) cudaFree(R.fr_mem);
+  R.fr_mem = mem;
+  R.fr_interval = interval;
+  R.fr_cap = interval > 0 ? capacity : 0;
+  R.fr_vel = with_velocities ? 1 : 0;
+  R.fr_written = R.fr_read = 0;
+  R.fr_steps.assign(R.fr_cap, -1);
+  return PRISMQ_OK;
+}
+
+prismq_status prismq_batch_frames_read(prismq_batch* b, int32_t slot, float* xyz, float* vxyz, int64_t* steps,
+                                       int32_t max_frames, int32_t* n_out, int64_t* dropped) {
+  prismq_status rc = check_slot(b, slot);
+  if (rc != PRISMQ_OK) return rc;
+  if (!n_out || max_frames < 0 || (max_frames > 0 && !xyz)) return fail(PRISMQ_E_INVALID, "invalid argument");
+  *n_out = 0;
+  if (dropped) *dropped = 0;
+  SlotRec& R = b->slots[slot];
+  if (R.fr_interval <= 0) return fail(PRISMQ_E_INVALID, "no trajectory frames configured");
+  if (vxyz && !R.fr_vel) return fail(PRISMQ_E_INVALID, "frames were configured without velocities");
+  if (R.fr_written - R.fr_read > R.fr_cap) {  // overwritten before they were read
+    if (dropped) *dropped = R.fr_written - R.fr_cap - R.fr_read;
+    R.fr_read = R.fr_written - R.fr_cap;
+  }
+  const int count = (int)std::min<int64_t>(R.fr_written - R.fr_read, max_frames);
+  const int n = (int)R.n_atoms;
+  for (int i = 0; i < count; ++i) {
+    const int64_t sl = (R.fr_read + i) % R.fr_cap;
+    const float4* src = R.fr_mem + sl * (R.fr_vel ? 2 : 1) * n;
+    k_xyz_to_aos<<<(n + 255) / 256, 256, 0, b->st>>>(b->d_stage, src, n);
+    PQ_CK(cudaMemcpyAsync(xyz + (size_t)i * 3 * n, b->d_stage, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, b->st));
+    if (vxyz) {
+      k_xyz_to_aos<<<(n + 255) / 256, 256, 0, b->st>>>(b->d_stage, src + n, n);
+      PQ_CK(cudaMemcpyAsync(vxyz + (size_t)i * 3 * n, b->d_stage, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost,
+                            b->st));
+    }
+    if (steps) steps[i] = R.fr_steps[sl];
+  }
+  PQ_CK(cudaGetLastError());
+  PQ_CK(cudaStreamSynchronize(b->st));
+  R.fr_read += count;
+  *n_out = count;
+  return PRISMQ_OK;
+}
+
+prismq_status prismq_frames_configure(prismq_system* sys, int32_t interval, int32_t capacity, int32_t with_velocities) {
+  if (!sys) return fail(PRISMQ_E_INVALID, "system is NULL");
+  return prismq_batch_frames_configure(sys->b, sys->slot, interval, capacity, with_velocities);
+}
+prismq_status prismq_frames_read(prismq_system* sys, float* xyz, float* vxyz, int64_t* steps, int32_t max_frames,
+                                 int32_t* n_out, int64_t* dropped) {
+  if (!sys) return fail(PRISMQ_E_INVALID, "system is NULL");
+  return prismq_batch_frames_read(sys->b, sys->slot, xyz, vxyz, steps, max_frames, n_out, dropped);
+}
+
+prismq_status prismq_checkpoint_size(prismq_system* sys, size_t* bytes) {
+  if (!sys) return fail(PRISMQ_E_INVALID, "system is NULL");
+  return prismq_batch_checkpoint_size(sys->b, sys->slot, bytes);
+}
+prismq_status prismq_checkpoint_save(prismq_system* sys, void* buf, size_t cap, size_t* written) {
+  if (!sys) return fail(PRISMQ_E_INVALID, "system is NULL");
+  return prismq_batch_checkpoint_save(sys->b, sys->slot, buf, cap, written);
+}
+prismq_status prismq_checkpoint_restore(prismq_system* sys, const void* buf, size_t len) {
+  if (!sys) return fail(PRISMQ_E_INVALID, "system is NULL");
+  return prismq_batch_checkpoint_restore(sys->b, sys->slot, buf, len);
 }
 
 }  // extern "C"

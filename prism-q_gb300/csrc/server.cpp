@@ -47,6 +47,8 @@ struct Job {
   float* vout = nullptr;
   double t_submit = 0.0, t_start = 0.0;
   int32_t slot = -1;
+  bool has_protocol = false;
+  prismq_protocol protocol{};
 };
 
 void copy_message(char* dst, size_t cap, const std::string& msg) {
@@ -103,7 +105,9 @@ struct prismq_server {
       pq::PreparedSystem* prep = j.prep;
       lk.unlock();
       int32_t slot = -1;
-      const prismq_status rc = pq::admit_prepared(batch, prep, &slot);
+      prismq_status rc = pq::admit_prepared(batch, prep, &slot);
+      if (rc == PRISMQ_OK && j.has_protocol && (rc = prismq_batch_set_protocol(batch, slot, &j.protocol)) != PRISMQ_OK)
+        prismq_batch_remove_system(batch, slot);
       const std::string msg = rc != PRISMQ_OK ? prismq_last_error() : "";
       lk.lock();
       if (rc == PRISMQ_OK) {
@@ -252,6 +256,11 @@ prismq_status prismq_server_submit(prismq_server* s, const prismq_job* job, int6
     pq::set_last_error("the server runs FP32 (production) jobs");
     return PRISMQ_E_INVALID;
   }
+  if (job->protocol) {  // validated here so a bad protocol fails the submit, not the job
+    float probe[3];
+    const prismq_status prc = prismq_protocol_eval(job->protocol, 1, probe);
+    if (prc != PRISMQ_OK) return prc;
+  }
   pq::PreparedSystem* prep = nullptr;
   const prismq_status rc = pq::prepare_system(job->topology, &job->params, &prep);
   if (rc != PRISMQ_OK) return rc;
@@ -269,6 +278,10 @@ prismq_status prismq_server_submit(prismq_server* s, const prismq_job* job, int6
   j.n_steps = j.remaining = job->n_steps;
   j.xout = job->positions_out;
   j.vout = job->velocities_out;
+  if (job->protocol) {
+    j.has_protocol = true;
+    j.protocol = *job->protocol;
+  }
   {
     std::lock_guard<std::mutex> g(s->mu);
     j.id = s->next_id++;

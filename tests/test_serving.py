@@ -38,7 +38,7 @@ def test_server_structs_match_the_header(pq):
     # sizes of the C structs on LP64 (x86-64 and aarch64): the ctypes mirrors
     # must agree or every field after the first mismatch is misread
     assert ctypes.sizeof(pq.ServerConfigStruct) == 16
-    assert ctypes.sizeof(pq.JobStruct) == 96
+    assert ctypes.sizeof(pq.JobStruct) == 104
     assert ctypes.sizeof(pq.ParamsStruct) == 56
     assert ctypes.sizeof(pq.JobResultStruct) == 216
     assert ctypes.sizeof(pq.ServerStatsStruct) == 96
@@ -159,3 +159,34 @@ def test_failing_job_does_not_disturb_the_others(gpu, mix, ala40):
     for jid, ref in ((ia, ref_a), (ib, ref_b)):
         assert res[jid].ok, res[jid].message
         assert np.array_equal(res[jid].positions, ref[0]) and np.array_equal(res[jid].velocities, ref[1])
+
+
+@pytest.mark.gpu
+def test_served_jobs_follow_their_protocols(gpu, mix):
+    """Each job runs its own protocol inside the shared batch, exactly as alone."""
+    protos = [gpu.Protocol(start_temp=100.0 + 40 * k, end_temp=300.0, cold_hold_steps=3 * k, ramp_steps=30,
+                           warm_hold_steps=20, cryo_enabled=bool(k % 2), equilibration_steps=25,
+                           equilibration_gamma=60.0, adaptive_dt=k % 2, current_step=k)
+              for k in range(len(mix))]
+    ref = []
+    for (t, p, n), pr in zip(mix, protos):
+        e = gpu.NhsAmberFusedEngine(t, p)
+        e.set_protocol(pr)
+        e.step(n)
+        ref.append((e.get_positions(), e.get_velocities()))
+        e.close()
+    with gpu.Server(1 << 30, chunk_steps=37) as srv:
+        ids = [srv.submit(t, n, p, tag=k, protocol=pr) for k, ((t, p, n), pr) in enumerate(zip(mix, protos))]
+        res = _drain(srv, len(ids))
+    for k, jid in enumerate(ids):
+        r = res[jid]
+        assert r.ok, r.message
+        assert np.array_equal(r.positions, ref[k][0]) and np.array_equal(r.velocities, ref[k][1])
+
+
+@pytest.mark.gpu
+def test_invalid_protocol_rejected_at_submit(gpu, mix):
+    bad = gpu.Protocol(adaptive_dt=5)
+    with gpu.Server(1 << 28) as srv:
+        with pytest.raises(gpu.PrismQError):
+            srv.submit(mix[0][0], 10, mix[0][1], protocol=bad)

@@ -18,7 +18,7 @@ def test_header_symbols_exported(pq):
     lib = pq.load()
     missing = [n for n in sorted(names) if not hasattr(lib, n)]
     assert not missing, missing
-    assert lib.prismq_abi_version() == 2
+    assert lib.prismq_abi_version() == 3
 
 
 def test_no_device_is_reported_not_faked(pq):
