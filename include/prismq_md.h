@@ -402,10 +402,15 @@ prismq_status prismq_batch_set_state_all(prismq_batch* b, const float* xyz, cons
 prismq_status prismq_batch_get_state_all(prismq_batch* b, float* xyz, float* vxyz);
 /* Advance every resident system by n_steps+1 steps, of which n_steps are
  * captured in one CUDA graph and timed on the device: total_ms covers those
- * n_steps; phase_ms (optional, 4*n_steps entries) holds, for step i at
- * [4i..4i+3], the device time of its control, neighbour-row, force and
- * integrate launches (events recorded between the launches). */
+ * n_steps; phase_ms (optional, 5*n_steps entries) holds, for step i at
+ * [5i..5i+4], the device time on the main stream of (decision + control),
+ * row builder, rebuilt systems' forces up to the join, noise + integrate,
+ * and then the other systems' force launch on the second stream, which
+ * overlaps the first three (events recorded between the launches). */
 prismq_status prismq_batch_run_timed(prismq_batch* b, int64_t n_steps, float* total_ms, float* phase_ms);
+/* Average device time of the force kernel over every resident system,
+ * launched alone n times on the main stream (the roofline's denominator). */
+prismq_status prismq_batch_time_force(prismq_batch* b, int32_t n_launches, float* ms_per_launch);
 int32_t prismq_batch_resident_systems(const prismq_batch* b);
 
 /* ---- job server: continuous batching of independent MD jobs ----

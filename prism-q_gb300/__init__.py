@@ -215,6 +215,7 @@ def load() -> ctypes.CDLL:
         "prismq_batch_set_state_all": (I, [P, P, P]),
         "prismq_batch_get_state_all": (I, [P, P, P]),
         "prismq_batch_run_timed": (I, [P, i64, P, P]),
+        "prismq_batch_time_force": (I, [P, ctypes.c_int32, P]),
         "prismq_batch_counters": (I, [P, ctypes.c_int32, P]),
         "prismq_batch_tuning": (I, [P, P]),
         "prismq_batch_create_ex": (I, [i64, ctypes.c_int32, ctypes.c_int32, P]),

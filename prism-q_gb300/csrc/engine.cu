@@ -706,6 +706,11 @@ struct prismq_batch {
   int n_check32 = 0, n_check64 = 0;  // resident FP32 systems by constraint-check precision
   int group_slots = 0;                // the largest force-group slot count among resident systems
   std::vector<SysDev> h_sys;
+  // Overlapped step: the branch-B force launch runs on st2 beside the list
+  // rebuild on st; st has the higher priority so that the rebuild's few,
+  // latency-bound blocks are scheduled ahead of the force launch's many.
+  cudaStream_t st2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 
   ~prismq_batch() {
     for (auto& r : slots)
@@ -717,6 +722,9 @@ struct prismq_batch {
                     A.pos64, A.vel64, A.f64, A.lj64, d_energy, d_stage, d_stage2, d_stage64};
     for (void* p : ptrs)
       if (p) cudaFree(p);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    if (st2) cudaStreamDestroy(st2);
     if (st) cudaStreamDestroy(st);
   }
 
@@ -773,11 +781,36 @@ struct prismq_batch {
     return 1 + (A.fp64 ? 1 : (n_check32 > 0 || n_check64 == 0 ? 1 : 0) + (n_check64 > 0 ? 1 : 0));
   }
 
-  void enqueue_step_body() {
+  // One step up to its forces.  k_decide chooses the systems that rebuild
+  // their lists (or remove their COM velocity) this step; on st their cells
+  // are sorted, their rows built and their forces evaluated, while on st2 the
+  // forces of every other system, which need none of that, are evaluated at
+  // the same time.  (Sorting the cells before the fork, on an empty GPU, was
+  // measured slower: 0.93 against 0.84 ms per step on 256 systems.)  Each system's forces come from exactly one of the two
+  // force launches, with the same code, so the results do not depend on the
+  // split.
+  // ev (optional, 4 events, captured as external records): before k_decide,
+  // after the control kernel, after the row builder, after the join.
+  // evb (optional, 2): around the branch-B force launch on st2.
+  prismq_status enqueue_step_body(cudaEvent_t* ev = nullptr, cudaEvent_t* evb = nullptr) {
+    if (ev) PQ_CK(cudaEventRecordWithFlags(ev[0], st, cudaEventRecordExternal));
+    launch_decide(A, sys_span, st);
+    PQ_CK(cudaEventRecord(ev_fork, st));
+    PQ_CK(cudaStreamWaitEvent(st2, ev_fork, 0));
+    if (evb) PQ_CK(cudaEventRecordWithFlags(evb[0], st2, cudaEventRecordExternal));
+    launch_force(A, atom_span, false, st2, kSelBranchB, force_variant, group_slots);
+    if (evb) PQ_CK(cudaEventRecordWithFlags(evb[1], st2, cudaEventRecordExternal));
     launch_control_cells(A, sys_span, kCtlStep, -1, st);
+    if (ev) PQ_CK(cudaEventRecordWithFlags(ev[1], st, cudaEventRecordExternal));
     launch_nbr_build(A, atom_span, 1, st);
-    launch_force(A, atom_span, false, st, false, force_variant, group_slots);
+    if (ev) PQ_CK(cudaEventRecordWithFlags(ev[2], st, cudaEventRecordExternal));
+    launch_force(A, atom_span, false, st, kSelBranchA, force_variant, group_slots);
+    PQ_CK(cudaEventRecord(ev_join, st2));
+    PQ_CK(cudaStreamWaitEvent(st, ev_join, 0));
+    if (ev) PQ_CK(cudaEventRecordWithFlags(ev[3], st, cudaEventRecordExternal));
+    return PRISMQ_OK;
   }
+  static constexpr int kStepBodyLaunches = 5;
 
   // Autotuner: time every force-kernel launch shape on the resident batch
   // (three launches each, CUDA events) and keep the fastest.  The shapes give
@@ -792,9 +825,9 @@ struct prismq_batch {
     float best = 3.4e38f;
     int pick = 0;
     for (int v = 0; v < force_variant_count(); ++v) {
-      launch_force(A, atom_span, false, st, false, v, group_slots);
+      launch_force(A, atom_span, false, st, kSelAll, v, group_slots);
       PQ_CK(cudaEventRecord(e0, st));
-      for (int r = 0; r < 3; ++r) launch_force(A, atom_span, false, st, false, v, group_slots);
+      for (int r = 0; r < 3; ++r) launch_force(A, atom_span, false, st, kSelAll, v, group_slots);
       PQ_CK(cudaEventRecord(e1, st));
       PQ_CK(cudaEventSynchronize(e1));
       float ms = 0.f;
@@ -823,10 +856,12 @@ struct prismq_batch {
     }
     cudaGraph_t g;
     PQ_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    enqueue_step_body();
+    prismq_status brc = enqueue_step_body();
     integrate(kIntBoth);
-    PQ_CK(cudaStreamEndCapture(st, &g));
-    cudaError_t e = cudaGraphInstantiate(&gexec, g, 0);
+    cudaError_t ce = cudaStreamEndCapture(st, &g);
+    if (brc != PRISMQ_OK) return brc;
+    PQ_CK(ce);
+    cudaError_t e = cudaGraphInstantiateWithFlags(&gexec, g, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(g);
     PQ_CK(e);
     graph_dirty = false;
@@ -845,7 +880,7 @@ struct prismq_batch {
   prismq_status prime_flagged() {
     launch_control_cells(A, sys_span, kCtlPrime, -1, st);
     launch_nbr_build(A, atom_span, 1, st);
-    launch_force(A, atom_span, false, st, true, 0, group_slots);
+    launch_force(A, atom_span, false, st, kSelRebuilding, 0, group_slots);
     g_launches += 3;
     PQ_CK(cudaGetLastError());
     for (auto& s : slots) s.need_prime = false;
@@ -873,35 +908,34 @@ struct prismq_batch {
     return fail(PRISMQ_E_NONFINITE, "non-finite state" + where);
   }
 
-  // n steady steps captured in one graph with an event pair around every force
-  // launch; head and tail phases run outside the timed graph.
-  // phase_ms (optional, 4*n entries): for step i the device time of the
-  // control, neighbour-row, force and integrate launches, from events recorded
-  // between consecutive launches inside the graph.
+  // n steady steps captured in one graph with events between the launches;
+  // head and tail phases run outside the timed graph.
+  // phase_ms (optional, 5*n entries): for step i the device time of
+  // [decide + control, row builder, branch-A forces up to the join,
+  // noise + integrate] on the main stream, then the branch-B force launch on
+  // the second stream (which overlaps the first three).
   prismq_status run_timed(int64_t n, float* total_ms, float* phase_ms) {
     if (n <= 0 || sys_span == 0) return fail(PRISMQ_E_INVALID, "nothing to time");
     prismq_status rc = prime_if_needed();
     if (rc != PRISMQ_OK) return rc;
     if ((rc = tune_force()) != PRISMQ_OK) return rc;
-    std::vector<cudaEvent_t> ev(4 * n + 1);
+    std::vector<cudaEvent_t> ev(4 * n + 1), evb(2 * n);
     for (auto& e : ev) PQ_CK(cudaEventCreate(&e));
+    for (auto& e : evb) PQ_CK(cudaEventCreate(&e));
     g_launches += integrate(kIntPre);
     cudaGraph_t g;
     cudaGraphExec_t ge = nullptr;
     PQ_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    for (int64_t i = 0; i < n; ++i) {
-      cudaEventRecordWithFlags(ev[4 * i + 0], st, cudaEventRecordExternal);
-      launch_control_cells(A, sys_span, kCtlStep, -1, st);
-      cudaEventRecordWithFlags(ev[4 * i + 1], st, cudaEventRecordExternal);
-      launch_nbr_build(A, atom_span, 1, st);
-      cudaEventRecordWithFlags(ev[4 * i + 2], st, cudaEventRecordExternal);
-      launch_force(A, atom_span, false, st, false, force_variant, group_slots);
-      cudaEventRecordWithFlags(ev[4 * i + 3], st, cudaEventRecordExternal);
+    prismq_status brc = PRISMQ_OK;
+    for (int64_t i = 0; i < n && brc == PRISMQ_OK; ++i) {
+      brc = enqueue_step_body(&ev[4 * i], &evb[2 * i]);
       integrate(kIntBoth);
     }
     cudaEventRecordWithFlags(ev[4 * n], st, cudaEventRecordExternal);
-    PQ_CK(cudaStreamEndCapture(st, &g));
-    cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+    cudaError_t ce = cudaStreamEndCapture(st, &g);
+    if (brc != PRISMQ_OK) return brc;
+    PQ_CK(ce);
+    cudaError_t e = cudaGraphInstantiateWithFlags(&ge, g, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(g);
     PQ_CK(e);
     PQ_CK(cudaStreamSynchronize(st));
@@ -909,17 +943,45 @@ struct prismq_batch {
     cudaError_t le = cudaGraphLaunch(ge, st);
     nvtxRangePop();
     PQ_CK(le);
-    g_launches += (3 + integrate_passes()) * n;
+    g_launches += (kStepBodyLaunches + integrate_passes()) * n;
     PQ_CK(cudaStreamSynchronize(st));
     PQ_CK(cudaEventElapsedTime(total_ms, ev[0], ev[4 * n]));
     if (phase_ms)
-      for (int64_t i = 0; i < 4 * n; ++i) PQ_CK(cudaEventElapsedTime(&phase_ms[i], ev[i], ev[i + 1]));
+      for (int64_t i = 0; i < n; ++i) {
+        for (int k = 0; k < 4; ++k) PQ_CK(cudaEventElapsedTime(&phase_ms[5 * i + k], ev[4 * i + k], ev[4 * i + k + 1]));
+        PQ_CK(cudaEventElapsedTime(&phase_ms[5 * i + 4], evb[2 * i], evb[2 * i + 1]));
+      }
     cudaGraphExecDestroy(ge);
     for (auto& x : ev) cudaEventDestroy(x);
-    enqueue_step_body();
-    g_launches += 3 + integrate(kIntPost);
+    for (auto& x : evb) cudaEventDestroy(x);
+    if ((rc = enqueue_step_body()) != PRISMQ_OK) return rc;
+    g_launches += kStepBodyLaunches + integrate(kIntPost);
     PQ_CK(cudaGetLastError());
     return check_status();
+  }
+
+  // The force kernel over every resident system, timed alone: n launches
+  // between two events on the main stream.
+  prismq_status time_force(int n, float* ms_per_launch) {
+    if (n <= 0 || sys_span == 0) return fail(PRISMQ_E_INVALID, "nothing to time");
+    prismq_status rc = prime_if_needed();
+    if (rc != PRISMQ_OK) return rc;
+    if ((rc = tune_force()) != PRISMQ_OK) return rc;
+    cudaEvent_t e0, e1;
+    PQ_CK(cudaEventCreate(&e0));
+    PQ_CK(cudaEventCreate(&e1));
+    launch_force(A, atom_span, false, st, kSelAll, force_variant, group_slots);  // warm
+    PQ_CK(cudaEventRecord(e0, st));
+    for (int i = 0; i < n; ++i) launch_force(A, atom_span, false, st, kSelAll, force_variant, group_slots);
+    PQ_CK(cudaEventRecord(e1, st));
+    PQ_CK(cudaEventSynchronize(e1));
+    float ms = 0.0f;
+    PQ_CK(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    g_launches += n + 1;
+    *ms_per_launch = ms / (float)n;
+    return PRISMQ_OK;
   }
 
   // Steps in segments that end on every trajectory-frame boundary of the
@@ -976,13 +1038,13 @@ struct prismq_batch {
     rc = ensure_graph();
     if (rc != PRISMQ_OK) return rc;
     g_launches += integrate(kIntPre);
-    const int per_step = 3 + integrate_passes();
+    const int per_step = kStepBodyLaunches + integrate_passes();
     for (int64_t i = 1; i < n; ++i) {
       PQ_CK(cudaGraphLaunch(gexec, st));
       g_launches += per_step;
     }
-    enqueue_step_body();
-    g_launches += 3 + integrate(kIntPost);
+    if ((rc = enqueue_step_body()) != PRISMQ_OK) return rc;
+    g_launches += kStepBodyLaunches + integrate(kIntPost);
     PQ_CK(cudaGetLastError());
     return check_status();
   }
@@ -1022,7 +1084,14 @@ prismq_status batch_alloc(prismq_batch* B, int64_t atom_cap, int sys_cap, int64_
   A.exc_cap = std::max<int64_t>(exc_cap, 1);
   A.gref_cap = std::max<int64_t>(gref_cap, 1);
   A.sys_cap = sys_cap;
-  if (!dry) PQ_CK(cudaStreamCreateWithFlags(&B->st, cudaStreamNonBlocking));
+  if (!dry) {
+    int lo = 0, hi = 0;
+    PQ_CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    PQ_CK(cudaStreamCreateWithPriority(&B->st, cudaStreamNonBlocking, hi));
+    PQ_CK(cudaStreamCreateWithPriority(&B->st2, cudaStreamNonBlocking, lo));
+    PQ_CK(cudaEventCreateWithFlags(&B->ev_fork, cudaEventDisableTiming));
+    PQ_CK(cudaEventCreateWithFlags(&B->ev_join, cudaEventDisableTiming));
+  }
 #define PQ_ALLOC(ptr, count)                                  \
   do {                                                        \
     const size_t nb_ = sizeof(*(ptr)) * (size_t)(count);      \
@@ -1361,10 +1430,10 @@ prismq_status check_slot(prismq_batch* B, int slot) {
 prismq_status eval_energy(prismq_batch* B, int slot, double* out15) {
   prismq_status rc = B->prime_if_needed();
   if (rc != PRISMQ_OK) return rc;
-  launch_force(B->A, B->atom_span, true, B->st, false, 0, B->group_slots);
+  launch_force(B->A, B->atom_span, true, B->st, kSelAll, 0, B->group_slots);
   launch_energy_reduce(B->A, B->sys_span, B->d_energy, B->st);
   // the stepping kernels consume forces from the force-only variant
-  launch_force(B->A, B->atom_span, false, B->st, false, 0, B->group_slots);
+  launch_force(B->A, B->atom_span, false, B->st, kSelAll, 0, B->group_slots);
   g_launches += 3;
   PQ_CK(cudaGetLastError());
   if (out15) {
@@ -1611,6 +1680,11 @@ prismq_status prismq_batch_energy(prismq_batch* b, int32_t slot, double out[6]) 
 prismq_status prismq_batch_run_timed(prismq_batch* b, int64_t n_steps, float* total_ms, float* phase_ms) {
   if (!b || !total_ms) return fail(PRISMQ_E_INVALID, "NULL argument");
   return b->run_timed(n_steps, total_ms, phase_ms);
+}
+
+prismq_status prismq_batch_time_force(prismq_batch* b, int32_t n_launches, float* ms_per_launch) {
+  if (!b || !ms_per_launch) return fail(PRISMQ_E_INVALID, "NULL argument");
+  return b->time_force(n_launches, ms_per_launch);
 }
 
 int64_t prismq_batch_atom_span(const prismq_batch* b) { return b ? b->atom_span : 0; }
@@ -1917,7 +1991,7 @@ prismq_status prismq_build_neighbors(prismq_system* sys, prismq_nlist_mode mode,
     return fail(PRISMQ_E_INVALID, "reference grid needs more than 32 cells per axis for this system");
   launch_control_cells(B->A, B->sys_span, kCtlForce, (int)mode, B->st);
   launch_nbr_build(B->A, B->atom_span, 0, B->st);
-  launch_force(B->A, B->atom_span, false, B->st, false, 0, B->group_slots);  // also clears the rebuild queue
+  launch_force(B->A, B->atom_span, false, B->st, kSelAll, 0, B->group_slots);  // also clears the rebuild queue
   g_launches += 3;
   PQ_CK(cudaGetLastError());
   const int64_t n = R.n_atoms, ab = R.atom_b;
@@ -1932,7 +2006,7 @@ prismq_status prismq_build_neighbors(prismq_system* sys, prismq_nlist_mode mode,
   // restore the production list
   launch_control_cells(B->A, B->sys_span, kCtlForce, 0, B->st);
   launch_nbr_build(B->A, B->atom_span, 1, B->st);
-  launch_force(B->A, B->atom_span, false, B->st, false, 0, B->group_slots);
+  launch_force(B->A, B->atom_span, false, B->st, kSelAll, 0, B->group_slots);
   g_launches += 3;
   PQ_CK(cudaGetLastError());
   PQ_CK(cudaStreamSynchronize(B->st));
@@ -2101,7 +2175,7 @@ prismq_status prismq_batch_checkpoint_restore(prismq_batch* b, int32_t slot, con
     PQ_CK(cudaMemcpyAsync(b->A.sys + slot, &S, sizeof(S), cudaMemcpyHostToDevice, b->st));
     if ((rc = b->prime_flagged()) != PRISMQ_OK) return rc;
     if ((rc = set_xyz(b, slot, b->A.pos, x)) != PRISMQ_OK) return rc;
-    launch_force(b->A, b->atom_span, false, b->st, true, 0, b->group_slots);
+    launch_force(b->A, b->atom_span, false, b->st, kSelRebuilding, 0, b->group_slots);
     g_launches += 1;
     PQ_CK(cudaGetLastError());
     if ((rc = b->sync_sys_from_device()) != PRISMQ_OK) return rc;

@@ -397,9 +397,10 @@ __device__ __forceinline__ bool exception_out(const R4<R>* pos, const ExcT e, Te
 // each term for every member atom (nhs_amber_fused.cu:3002-3090); evaluating
 // it once per group gives each member the same contribution.
 template <class R, bool kEnergy, int kMinBlocks>
-__global__ void __launch_bounds__(128, kMinBlocks) k_force(Arena A, int64_t n_span, int only_rebuilt, int cap) {
+__global__ void __launch_bounds__(128, kMinBlocks) k_force(Arena A, int64_t n_span, int sel, int cap) {
   // the row builder that ran before this launch consumed the rebuild queue
-  if (blockIdx.x == 0 && threadIdx.x == 0) A.work_ctl[0] = 0;
+  // (the branch-B launch of an overlapped step may run beside that builder)
+  if (sel != kSelBranchB && blockIdx.x == 0 && threadIdx.x == 0) A.work_ctl[0] = 0;
   extern __shared__ __align__(16) unsigned char force_smem[];
   __shared__ int s_base[kForceGroup], s_nb[kForceGroup], s_na[kForceGroup], s_nd[kForceGroup];
   const int tid = threadIdx.x, q = tid & 3;
@@ -408,7 +409,10 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_force(Arena A, int64_t n_sp
   const int s0 = A.atom_sys[a0];
   if (s0 < 0) return;
   const SysDev* Sp = &A.sys[s0];
-  if (!Sp->active || (only_rebuilt && !Sp->rebuilding)) return;  // whole block leaves together
+  if (!Sp->active) return;  // whole block leaves together
+  if (sel == kSelRebuilding && !Sp->rebuilding) return;
+  if (sel == kSelBranchA && !Sp->branch_a) return;
+  if (sel == kSelBranchB && Sp->branch_a) return;
   R* slot_x = reinterpret_cast<R*>(force_smem);
   R* slot_y = slot_x + cap;
   R* slot_z = slot_y + cap;
@@ -649,10 +653,10 @@ static void force_launch(const Arena& A, int64_t n, int ob, int cap, cudaStream_
   k_force<R, kEnergy, kMinBlocks><<<blocks, 128, smem, st>>>(A, n, ob, cap);
 }
 
-void launch_force(const Arena& A, int64_t n_atoms_span, bool energy, cudaStream_t st, bool only_rebuilt,
-                  int variant, int group_slots) {
+void launch_force(const Arena& A, int64_t n_atoms_span, bool energy, cudaStream_t st, int sel, int variant,
+                  int group_slots) {
   if (n_atoms_span <= 0) return;
-  const int ob = only_rebuilt ? 1 : 0;
+  const int ob = sel;
   const int cap = (std::max(group_slots, 1) + 7) & ~7;  // keeps the FP64 energy plane 8-byte aligned
   if (A.fp64) {
     if (energy)

@@ -145,6 +145,62 @@ __device__ __noinline__ void com_pre(const Arena& A, SysDev* Sp, long long st, l
   __syncthreads();
 }
 
+// The schedule decision of one step: rebuild the list or not (interval or
+// half-skin displacement), advance the step counter, keep this step's
+// parameters for its post-force phases and, under a protocol, evaluate the
+// director for the next step's pre-force phases (protocol_director.cu:54-143).
+__device__ bool decide_step(SysDev* Sp, int disp, int status) {
+  bool rb = !Sp->built || disp || Sp->steps_since_rebuild >= Sp->rebuild_interval;
+  Sp->step = Sp->step + 1;
+  Sp->post_dt = Sp->dt;
+  Sp->post_temperature = Sp->temperature;
+  Sp->post_gamma = Sp->gamma;
+  Sp->post_c1 = Sp->c1;
+  Sp->post_c1d = Sp->c1d;
+  if (Sp->proto.on) {
+    StepParams P;
+    protocol_eval(Sp->proto, Sp->step - Sp->proto.origin, &P);
+    Sp->dt = P.dt;
+    Sp->temperature = P.temperature;
+    Sp->gamma = P.gamma;
+    Sp->c1 = P.c1;
+    Sp->c1d = P.c1d;
+  }
+  if (status != 0) rb = false;
+  Sp->steps_since_rebuild = rb ? 1 : Sp->steps_since_rebuild + 1;
+  Sp->displaced = 0;
+  Sp->rebuilding = rb ? 1 : 0;
+  if (rb) Sp->n_rebuilds += 1;
+  return rb;
+}
+
+// One thread per system at the start of every step.  Systems at a COM step
+// are left to the control kernel, which removes the COM velocity and runs
+// their deferred pre-force phases before it decides.
+__global__ void __launch_bounds__(128) k_decide(Arena A, int n_sys) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n_sys) return;
+  SysDev* Sp = &A.sys[s];
+  if (!Sp->active) return;
+  if (Sp->status != 0) {
+    Sp->branch_a = 0;
+    return;
+  }
+  const long long st = Sp->step;
+  if (Sp->com_interval > 0 && st > 0 && (st % Sp->com_interval) == 0) {
+    Sp->com_pending = 1;
+    Sp->branch_a = 1;
+    return;
+  }
+  Sp->com_pending = 0;
+  Sp->branch_a = decide_step(Sp, Sp->displaced, 0) ? 1 : 0;
+}
+
+void launch_decide(const Arena& A, int n_sys, cudaStream_t st) {
+  if (n_sys <= 0) return;
+  k_decide<<<(n_sys + 127) / 128, 128, 0, st>>>(A, n_sys);
+}
+
 __global__ void __launch_bounds__(kCtlThreads) k_control_cells(Arena A, int mode, int nbr_override) {
   extern __shared__ int sm[];  // per-warp sort scratch: 32 * kCellSortCap ints
   __shared__ long long red_i[3][32];
@@ -158,11 +214,13 @@ __global__ void __launch_bounds__(kCtlThreads) k_control_cells(Arena A, int mode
   if (!Sp->active) return;
   if (Sp->status != 0) return;
   const int ab = Sp->atom_begin, na = Sp->n_atoms;
+  // in a step, k_decide has already decided for every system not at a COM step
+  const bool decided = mode == kCtlStep && !Sp->com_pending;
+  if (decided && !Sp->rebuilding) return;
 
-  if (mode == kCtlStep) {
+  if (mode == kCtlStep && !decided) {
     const long long st = Sp->step;
-    const bool com = Sp->com_interval > 0 && st > 0 && (st % Sp->com_interval) == 0;
-    if (com) {
+    {
       if (A.fp64)
         com_pre<double, false>(A, Sp, st, red_i, red_d, sh_vcomd);
       else if (Sp->check64)
@@ -174,45 +232,31 @@ __global__ void __launch_bounds__(kCtlThreads) k_control_cells(Arena A, int mode
 
   if (tid == 0) {
     bool rb;
-    const int disp = atomicAdd(&Sp->displaced, 0);
-    if (mode == kCtlPrime) {
-      rb = Sp->need_prime != 0;
-      Sp->need_prime = 0;
-    } else if (mode == kCtlForce) {
-      rb = true;
+    if (decided) {
+      rb = true;  // k_decide chose a rebuild
+    } else if (mode == kCtlStep) {
+      // a COM step: decide after the pre-force phases ran above
+      rb = decide_step(Sp, atomicAdd(&Sp->displaced, 0), atomicAdd(&Sp->status, 0));
+      Sp->com_pending = 0;
     } else {
-      rb = !Sp->built || disp || Sp->steps_since_rebuild >= Sp->rebuild_interval;
-      Sp->step = Sp->step + 1;
-      // This launch's integrate runs the post-force phases of the step just
-      // begun and the pre-force phases of the next one: keep this step's
-      // parameters for the former and, under a protocol, evaluate the
-      // director for the latter (protocol_director.cu:54-143).
-      Sp->post_dt = Sp->dt;
-      Sp->post_temperature = Sp->temperature;
-      Sp->post_gamma = Sp->gamma;
-      Sp->post_c1 = Sp->c1;
-      Sp->post_c1d = Sp->c1d;
-      if (Sp->proto.on) {
-        StepParams P;
-        protocol_eval(Sp->proto, Sp->step - Sp->proto.origin, &P);
-        Sp->dt = P.dt;
-        Sp->temperature = P.temperature;
-        Sp->gamma = P.gamma;
-        Sp->c1 = P.c1;
-        Sp->c1d = P.c1d;
+      if (mode == kCtlPrime) {
+        rb = Sp->need_prime != 0;
+        Sp->need_prime = 0;
+      } else {
+        rb = true;
       }
+      if (atomicAdd(&Sp->status, 0) != 0) rb = false;
+      // A prime pass (another system was admitted or reset) leaves the
+      // schedule of the systems it does not rebuild untouched, so a system's
+      // trajectory never depends on what else shares the batch.
+      if (mode != kCtlPrime || rb) {
+        Sp->steps_since_rebuild = rb ? 1 : Sp->steps_since_rebuild + 1;
+        Sp->displaced = 0;
+      }
+      Sp->rebuilding = rb ? 1 : 0;
+      if (rb) Sp->n_rebuilds += 1;
+      if (nbr_override >= 0 && rb) Sp->nbr_mode = nbr_override;
     }
-    if (atomicAdd(&Sp->status, 0) != 0) rb = false;
-    // A prime pass (another system was admitted or reset) leaves the schedule
-    // of the systems it does not rebuild untouched, so a system's trajectory
-    // never depends on what else shares the batch.
-    if (mode != kCtlPrime || rb) {
-      Sp->steps_since_rebuild = rb ? 1 : Sp->steps_since_rebuild + 1;
-      Sp->displaced = 0;
-    }
-    Sp->rebuilding = rb ? 1 : 0;
-    if (rb) Sp->n_rebuilds += 1;
-    if (nbr_override >= 0 && rb) Sp->nbr_mode = nbr_override;
     sh_rb = rb ? 1 : 0;
   }
   __syncthreads();

@@ -118,6 +118,12 @@ struct SysDev {
   float post_dt, post_temperature, post_gamma, post_c1;
   double post_c1d;
   ProtocolDev proto;  // proto.on: the control kernel evaluates T, γ, dt every step
+  // Set by k_decide at the start of a step.  branch_a: the system's forces
+  // wait for this step's control and row-building launches (it rebuilds its
+  // list, or its COM removal and pre-force phases run in the control
+  // kernel); the other systems' forces run concurrently with those launches.
+  int branch_a;
+  int com_pending;  // this step removes the COM velocity in the control kernel
 };
 
 // Per-atom incidence into bonded term arrays (reference: atom_bond_list etc.,
@@ -196,12 +202,18 @@ constexpr int kIntBoth = 3;
 // launchers (nbr.cu, force.cu, integrate.cu)
 void launch_control_cells(const Arena& A, int n_sys, int mode, int nbr_mode_override,
                           cudaStream_t st);
+// The per-system schedule decision of a step (one thread per system).
+void launch_decide(const Arena& A, int n_sys, cudaStream_t st);
+// Force launch selections.
+constexpr int kSelAll = 0, kSelRebuilding = 1, kSelBranchA = 2, kSelBranchB = 3;
 void launch_nbr_build(const Arena& A, int64_t n_atoms_span, int exclude_exceptions,
                       cudaStream_t st);
 // group_slots: the largest number of bonded + exception incidences of one
 // 32-atom group among the resident systems (sizes the shared-memory slots).
+// sel: kSelAll, kSelRebuilding (systems rebuilt by the preceding control
+// pass), kSelBranchA / kSelBranchB (the two halves of an overlapped step).
 void launch_force(const Arena& A, int64_t n_atoms_span, bool energy, cudaStream_t st,
-                  bool only_rebuilt = false, int variant = 0, int group_slots = 0);
+                  int sel = kSelAll, int variant = 0, int group_slots = 0);
 int force_variant_count();
 void force_variant_shape(int variant, int* block, int* min_blocks);
 // check64_pass: 0 = systems with FP32 constraint checks, 1 = systems with FP64
