@@ -705,6 +705,7 @@ struct prismq_batch {
   int precision = PRISMQ_PRECISION_FP32;
   int n_check32 = 0, n_check64 = 0;  // resident FP32 systems by constraint-check precision
   int group_slots = 0;                // the largest force-group slot count among resident systems
+  int64_t max_big_atoms = 0;          // the largest resident system of >= kBigSortAtoms atoms (0: none)
   std::vector<SysDev> h_sys;
   // Overlapped step: the branch-B force launch runs on st2 beside the list
   // rebuild on st; st has the higher priority so that the rebuild's few,
@@ -718,7 +719,7 @@ struct prismq_batch {
     if (gexec) cudaGraphExecDestroy(gexec);
     void* ptrs[] = {A.pos, A.vel, A.lj, A.xref, A.f, A.pe, A.atom_sys, A.mask_all, A.mask_ref, A.far,
                     A.far_list, A.inc, A.inc_list, A.ex_idx, A.ex_partner, A.ex_par, A.exc, A.grp, A.grp_refs, A.bonds, A.angles,
-                    A.dihs, A.units, A.noise, A.nbr, A.nnbr, A.cell_start, A.cell_atoms, A.atom_cell, A.work, A.work_ctl, A.sys,
+                    A.dihs, A.units, A.noise, A.nbr, A.nnbr, A.cell_start, A.cell_atoms, A.atom_cell, A.work, A.work_ctl, A.big_list, A.sys,
                     A.pos64, A.vel64, A.f64, A.lj64, d_energy, d_stage, d_stage2, d_stage64};
     for (void* p : ptrs)
       if (p) cudaFree(p);
@@ -728,19 +729,29 @@ struct prismq_batch {
     if (st) cudaStreamDestroy(st);
   }
 
+  // The control kernel, followed for large systems by the grid-wide cell sort.
+  void control(int mode, int nbr_override, cudaStream_t s) {
+    launch_control_cells(A, sys_span, mode, nbr_override, s);
+    launch_big_cells(A, max_big_atoms, s);
+  }
+
   void update_spans() {
     const int64_t na = r_atoms.high(), nu = r_units.high();
     int ns = 0;
     int c32 = 0, c64 = 0;
     int gs = 0;
+    int64_t big = 0;
     for (int i = 0; i < (int)slots.size(); ++i)
       if (slots[i].active) {
+        if (slots[i].n_atoms >= kBigSortAtoms) big = std::max(big, slots[i].n_atoms);
         ns = i + 1;
         (slots[i].params.constraint_check_fp64 ? c64 : c32) += 1;
         gs = std::max(gs, slots[i].max_group_slots);
       }
     if (gs != group_slots) graph_dirty = true;
     group_slots = gs;
+    if (big != max_big_atoms) graph_dirty = true;
+    max_big_atoms = big;
     if (na != atom_span || nu != unit_span || ns != sys_span) graph_dirty = true;
     if ((c32 > 0) != (n_check32 > 0) || (c64 > 0) != (n_check64 > 0)) graph_dirty = true;
     n_check32 = c32;
@@ -800,7 +811,7 @@ struct prismq_batch {
     if (evb) PQ_CK(cudaEventRecordWithFlags(evb[0], st2, cudaEventRecordExternal));
     launch_force(A, atom_span, false, st2, kSelBranchB, force_variant, group_slots);
     if (evb) PQ_CK(cudaEventRecordWithFlags(evb[1], st2, cudaEventRecordExternal));
-    launch_control_cells(A, sys_span, kCtlStep, -1, st);
+    control(kCtlStep, -1, st);
     if (ev) PQ_CK(cudaEventRecordWithFlags(ev[1], st, cudaEventRecordExternal));
     launch_nbr_build(A, atom_span, 1, st);
     if (ev) PQ_CK(cudaEventRecordWithFlags(ev[2], st, cudaEventRecordExternal));
@@ -810,7 +821,7 @@ struct prismq_batch {
     if (ev) PQ_CK(cudaEventRecordWithFlags(ev[3], st, cudaEventRecordExternal));
     return PRISMQ_OK;
   }
-  static constexpr int kStepBodyLaunches = 5;
+  int body_launches() const { return 5 + (max_big_atoms > 0 ? 4 : 0); }
 
   // Autotuner: time every force-kernel launch shape on the resident batch
   // (three launches each, CUDA events) and keep the fastest.  The shapes give
@@ -878,10 +889,10 @@ struct prismq_batch {
 
   // Refresh lists and forces of the systems whose device need_prime flag is set.
   prismq_status prime_flagged() {
-    launch_control_cells(A, sys_span, kCtlPrime, -1, st);
+    control(kCtlPrime, -1, st);
     launch_nbr_build(A, atom_span, 1, st);
     launch_force(A, atom_span, false, st, kSelRebuilding, 0, group_slots);
-    g_launches += 3;
+    g_launches += 3 + (max_big_atoms > 0 ? 4 : 0);
     PQ_CK(cudaGetLastError());
     for (auto& s : slots) s.need_prime = false;
     return PRISMQ_OK;
@@ -943,7 +954,7 @@ struct prismq_batch {
     cudaError_t le = cudaGraphLaunch(ge, st);
     nvtxRangePop();
     PQ_CK(le);
-    g_launches += (kStepBodyLaunches + integrate_passes()) * n;
+    g_launches += (body_launches() + integrate_passes()) * n;
     PQ_CK(cudaStreamSynchronize(st));
     PQ_CK(cudaEventElapsedTime(total_ms, ev[0], ev[4 * n]));
     if (phase_ms)
@@ -955,7 +966,7 @@ struct prismq_batch {
     for (auto& x : ev) cudaEventDestroy(x);
     for (auto& x : evb) cudaEventDestroy(x);
     if ((rc = enqueue_step_body()) != PRISMQ_OK) return rc;
-    g_launches += kStepBodyLaunches + integrate(kIntPost);
+    g_launches += body_launches() + integrate(kIntPost);
     PQ_CK(cudaGetLastError());
     return check_status();
   }
@@ -1038,13 +1049,13 @@ struct prismq_batch {
     rc = ensure_graph();
     if (rc != PRISMQ_OK) return rc;
     g_launches += integrate(kIntPre);
-    const int per_step = kStepBodyLaunches + integrate_passes();
+    const int per_step = body_launches() + integrate_passes();
     for (int64_t i = 1; i < n; ++i) {
       PQ_CK(cudaGraphLaunch(gexec, st));
       g_launches += per_step;
     }
     if ((rc = enqueue_step_body()) != PRISMQ_OK) return rc;
-    g_launches += kStepBodyLaunches + integrate(kIntPost);
+    g_launches += body_launches() + integrate(kIntPost);
     PQ_CK(cudaGetLastError());
     return check_status();
   }
@@ -1128,6 +1139,7 @@ prismq_status batch_alloc(prismq_batch* B, int64_t atom_cap, int sys_cap, int64_
   PQ_ALLOC(A.cell_atoms, atom_cap);
   PQ_ALLOC(A.atom_cell, atom_cap);
   PQ_ALLOC(A.work, atom_cap / 8 + sys_cap + 1);
+  PQ_ALLOC(A.big_list, sys_cap);
   PQ_ALLOC(A.work_ctl, 4);
   PQ_ALLOC(A.sys, sys_cap);
   PQ_ALLOC(B->d_energy, kEnergyOut * (int64_t)sys_cap);
@@ -1989,10 +2001,10 @@ prismq_status prismq_build_neighbors(prismq_system* sys, prismq_nlist_mode mode,
   const SlotRec& R = B->slots[sys->slot];
   if (mode == PRISMQ_NLIST_REF27 && !R.ref_ok)
     return fail(PRISMQ_E_INVALID, "reference grid needs more than 32 cells per axis for this system");
-  launch_control_cells(B->A, B->sys_span, kCtlForce, (int)mode, B->st);
+  B->control(kCtlForce, (int)mode, B->st);
   launch_nbr_build(B->A, B->atom_span, 0, B->st);
   launch_force(B->A, B->atom_span, false, B->st, kSelAll, 0, B->group_slots);  // also clears the rebuild queue
-  g_launches += 3;
+  g_launches += 3 + (B->max_big_atoms > 0 ? 4 : 0);
   PQ_CK(cudaGetLastError());
   const int64_t n = R.n_atoms, ab = R.atom_b;
   std::vector<int> cnt(n);
@@ -2004,10 +2016,10 @@ prismq_status prismq_build_neighbors(prismq_system* sys, prismq_nlist_mode mode,
   PQ_CK(cudaStreamSynchronize(B->st));
   prismq_status st = B->check_status(sys->slot);
   // restore the production list
-  launch_control_cells(B->A, B->sys_span, kCtlForce, 0, B->st);
+  B->control(kCtlForce, 0, B->st);
   launch_nbr_build(B->A, B->atom_span, 1, B->st);
   launch_force(B->A, B->atom_span, false, B->st, kSelAll, 0, B->group_slots);
-  g_launches += 3;
+  g_launches += 3 + (B->max_big_atoms > 0 ? 4 : 0);
   PQ_CK(cudaGetLastError());
   PQ_CK(cudaStreamSynchronize(B->st));
   if (st != PRISMQ_OK) return st;

@@ -400,7 +400,10 @@ template <class R, bool kEnergy, int kMinBlocks>
 __global__ void __launch_bounds__(128, kMinBlocks) k_force(Arena A, int64_t n_span, int sel, int cap) {
   // the row builder that ran before this launch consumed the rebuild queue
   // (the branch-B launch of an overlapped step may run beside that builder)
-  if (sel != kSelBranchB && blockIdx.x == 0 && threadIdx.x == 0) A.work_ctl[0] = 0;
+  if (sel != kSelBranchB && blockIdx.x == 0 && threadIdx.x == 0) {
+    A.work_ctl[0] = 0;
+    A.work_ctl[1] = 0;
+  }
   extern __shared__ __align__(16) unsigned char force_smem[];
   __shared__ int s_base[kForceGroup], s_nb[kForceGroup], s_na[kForceGroup], s_nd[kForceGroup];
   const int tid = threadIdx.x, q = tid & 3;

@@ -44,6 +44,68 @@ __device__ __forceinline__ int cell_coord(float x, float lo, float inv_edge, int
   return c < 0 ? 0 : (c > n - 1 ? n - 1 : c);
 }
 
+// The cell of a position on the system's current grid.
+__device__ __forceinline__ int cell_of(const float4 p, int nbr_mode, const float (&lo)[3], const float (&inv_edge)[3],
+                                       const int (&dims)[3]) {
+  int ix, iy, iz;
+  if (nbr_mode == 1) {
+    // reference rule: truncate (x - origin) * 0.1f toward zero, then clamp
+    ix = (int)((p.x - lo[0]) * 0.1f);
+    iy = (int)((p.y - lo[1]) * 0.1f);
+    iz = (int)((p.z - lo[2]) * 0.1f);
+    ix = max(0, min(ix, dims[0] - 1));
+    iy = max(0, min(iy, dims[1] - 1));
+    iz = max(0, min(iz, dims[2] - 1));
+  } else {
+    ix = cell_coord(p.x, lo[0], inv_edge[0], dims[0]);
+    iy = cell_coord(p.y, lo[1], inv_edge[1], dims[1]);
+    iz = cell_coord(p.z, lo[2], inv_edge[2], dims[2]);
+  }
+  return ix + iy * dims[0] + iz * dims[0] * dims[1];
+}
+
+// The grid a system's last control pass chose (REF27: the fixed reference grid).
+__device__ __forceinline__ void grid_of(const SysDev* Sp, float (&lo)[3], float (&inv_edge)[3], int (&dims)[3]) {
+  for (int d = 0; d < 3; ++d) {
+    if (Sp->nbr_mode == 1) {
+      lo[d] = Sp->ref_origin[d];
+      inv_edge[d] = 0.1f;
+      dims[d] = Sp->ref_dims[d];
+    } else {
+      lo[d] = Sp->g_lo[d];
+      inv_edge[d] = Sp->g_inv_edge[d];
+      dims[d] = Sp->g_dims[d];
+    }
+  }
+}
+
+// Ascending order of one cell's atoms, by one warp (bitonic in its scratch).
+__device__ __forceinline__ void sort_cell(int* cell, int n, int* buf, int lane) {
+  if (n <= 1) return;
+  int p2 = 1;
+  while (p2 < n) p2 <<= 1;
+  for (int k = lane; k < p2; k += 32) buf[k] = k < n ? cell[k] : 0x7fffffff;
+  __syncwarp();
+  for (int w = 2; w <= p2; w <<= 1) {
+    for (int st = w >> 1; st > 0; st >>= 1) {
+      for (int k = lane; k < p2; k += 32) {
+        const int q = k ^ st;
+        if (q > k) {
+          const int x = buf[k], y = buf[q];
+          const bool up = (k & w) == 0;
+          if ((up && x > y) || (!up && x < y)) {
+            buf[k] = y;
+            buf[q] = x;
+          }
+        }
+      }
+      __syncwarp();
+    }
+  }
+  for (int k = lane; k < n; k += 32) cell[k] = buf[k];
+  __syncwarp();
+}
+
 // COM-velocity removal of one system followed by its deferred pre-phase
 // (every com_interval steps; housekeeping.cu:128-183 reduces with FP32
 // atomics).  FP32 systems sum m·v as exact int64 fixed point and m exactly in
@@ -343,24 +405,22 @@ __global__ void __launch_bounds__(kCtlThreads) k_control_cells(Arena A, int mode
   // ---- counting sort ----
   for (int c = tid; c <= ncell; c += kCtlThreads) start[c] = 0;
   __syncthreads();
+  if (na >= kBigSortAtoms) {
+    // a large system: the grid-wide kernels that follow sort its cells
+    __shared__ int sh_base_big;
+    const int ngroups = (na + 7) >> 3;
+    if (tid == 0) {
+      Sp->built = 1;
+      A.big_list[atomicAdd(&A.work_ctl[1], 1)] = s;
+      sh_base_big = atomicAdd(&A.work_ctl[0], ngroups);
+    }
+    __syncthreads();
+    for (int i = tid; i < ngroups; i += kCtlThreads) A.work[sh_base_big + i] = (ab >> 3) + i;
+    return;
+  }
   for (int i = tid; i < na; i += kCtlThreads) {
     const int a = ab + i;
-    const float4 p = A.pos[a];
-    int ix, iy, iz;
-    if (nbr_mode == 1) {
-      // reference rule: truncate (x - origin) * 0.1f toward zero, then clamp
-      ix = (int)((p.x - lo[0]) * 0.1f);
-      iy = (int)((p.y - lo[1]) * 0.1f);
-      iz = (int)((p.z - lo[2]) * 0.1f);
-      ix = max(0, min(ix, dims[0] - 1));
-      iy = max(0, min(iy, dims[1] - 1));
-      iz = max(0, min(iz, dims[2] - 1));
-    } else {
-      ix = cell_coord(p.x, lo[0], inv_edge[0], dims[0]);
-      iy = cell_coord(p.y, lo[1], inv_edge[1], dims[1]);
-      iz = cell_coord(p.z, lo[2], inv_edge[2], dims[2]);
-    }
-    const int c = ix + iy * dims[0] + iz * dims[0] * dims[1];
+    const int c = cell_of(A.pos[a], nbr_mode, lo, inv_edge, dims);
     A.atom_cell[a] = c;
     atomicAdd(&start[c + 1], 1);
   }
@@ -412,30 +472,8 @@ __global__ void __launch_bounds__(kCtlThreads) k_control_cells(Arena A, int mode
   // ---- ascending order inside each cell (warp per cell, bitonic in smem) ----
   int* buf = sm + warp * kCellSortCap;
   for (int c = warp; c < ncell; c += kCtlThreads / 32) {
-    const int b = start[c], e = start[c + 1], n = e - b;
-    if (n <= 1) continue;
-    int p2 = 1;
-    while (p2 < n) p2 <<= 1;
-    for (int k = lane; k < p2; k += 32) buf[k] = k < n ? A.cell_atoms[ab + b + k] : 0x7fffffff;
-    __syncwarp();
-    for (int w = 2; w <= p2; w <<= 1) {
-      for (int st = w >> 1; st > 0; st >>= 1) {
-        for (int k = lane; k < p2; k += 32) {
-          const int q = k ^ st;
-          if (q > k) {
-            const int x = buf[k], y = buf[q];
-            const bool up = (k & w) == 0;
-            if ((up && x > y) || (!up && x < y)) {
-              buf[k] = y;
-              buf[q] = x;
-            }
-          }
-        }
-        __syncwarp();
-      }
-    }
-    for (int k = lane; k < n; k += 32) A.cell_atoms[ab + b + k] = buf[k];
-    __syncwarp();
+    const int b = start[c];
+    sort_cell(A.cell_atoms + ab + b, start[c + 1] - b, buf, lane);
   }
   // queue this system's 8-atom groups for the row builder
   __shared__ int sh_base;
@@ -761,6 +799,126 @@ __global__ void __launch_bounds__(kNbrThreads, 3) k_nbr_build(Arena A, int64_t n
       build_group(A, g, exclude_exc, lane, sh[warp]);
     }
   }
+}
+
+// ---- the cell sort of large systems, grid-wide (a system of 100,000 atoms
+// has ~50,000 cells: one CTA would walk them in sequence).  The same cell
+// assignment, prefix sum and per-cell order as the single-CTA path, so the
+// rows that follow are identical. ----
+constexpr int kBigThreads = 256;
+
+__global__ void __launch_bounds__(kBigThreads) k_big_count(Arena A) {
+  const int nb = A.work_ctl[1];
+  for (int k = 0; k < nb; ++k) {
+    const SysDev* Sp = &A.sys[A.big_list[k]];
+    float lo[3], iv[3];
+    int dims[3];
+    grid_of(Sp, lo, iv, dims);
+    int* start = A.cell_start + Sp->cell_begin;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < Sp->n_atoms; i += gridDim.x * blockDim.x) {
+      const int a = Sp->atom_begin + i;
+      const int c = cell_of(A.pos[a], Sp->nbr_mode, lo, iv, dims);
+      A.atom_cell[a] = c;
+      atomicAdd(&start[c + 1], 1);
+    }
+  }
+}
+
+// One block per large system: the exclusive prefix over its cells, each
+// thread over a contiguous chunk, then a block-wide scan of the chunk sums.
+__global__ void __launch_bounds__(1024) k_big_scan(Arena A) {
+  __shared__ int wsum[32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nb = A.work_ctl[1];
+  for (int k = blockIdx.x; k < nb; k += gridDim.x) {
+    SysDev* Sp = &A.sys[A.big_list[k]];
+    const int nc = Sp->nbr_mode == 1 ? Sp->ref_dims[0] * Sp->ref_dims[1] * Sp->ref_dims[2]
+                                     : Sp->g_dims[0] * Sp->g_dims[1] * Sp->g_dims[2];
+    int* start = A.cell_start + Sp->cell_begin;
+    int* cursor = start + (Sp->cell_cap + 1);
+    const int chunk = (nc + 1023) / 1024;
+    const int c0 = min(tid * chunk, nc), c1 = min(c0 + chunk, nc);
+    int sum = 0;
+    bool ovf = false;
+    for (int c = c0; c < c1; ++c) {
+      const int v = start[c + 1];
+      ovf |= v > kCellSortCap;
+      sum += v;
+    }
+    if (ovf) atomicOr(&Sp->status, kStCellOverflow);
+    int x = sum;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      int w = wsum[lane];
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += y;
+      }
+      wsum[lane] = w;
+    }
+    __syncthreads();
+    int run = x - sum + (warp > 0 ? wsum[warp - 1] : 0);  // cells before c0
+    for (int c = c0; c < c1; ++c) {
+      const int v = start[c + 1];
+      cursor[c] = run;
+      run += v;
+      start[c + 1] = run;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kBigThreads) k_big_scatter(Arena A) {
+  const int nb = A.work_ctl[1];
+  for (int k = 0; k < nb; ++k) {
+    const SysDev* Sp = &A.sys[A.big_list[k]];
+    if (Sp->status != 0) continue;
+    int* cursor = A.cell_start + Sp->cell_begin + (Sp->cell_cap + 1);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < Sp->n_atoms; i += gridDim.x * blockDim.x) {
+      const int a = Sp->atom_begin + i;
+      const int slot = atomicAdd(&cursor[A.atom_cell[a]], 1);
+      A.cell_atoms[Sp->atom_begin + slot] = a;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kBigThreads) k_big_sort(Arena A) {
+  extern __shared__ int sm[];  // per-warp scratch: 8 * kCellSortCap ints
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nb = A.work_ctl[1];
+  int* buf = sm + warp * kCellSortCap;
+  for (int k = 0; k < nb; ++k) {
+    const SysDev* Sp = &A.sys[A.big_list[k]];
+    if (Sp->status != 0) continue;
+    const int nc = Sp->nbr_mode == 1 ? Sp->ref_dims[0] * Sp->ref_dims[1] * Sp->ref_dims[2]
+                                     : Sp->g_dims[0] * Sp->g_dims[1] * Sp->g_dims[2];
+    const int* start = A.cell_start + Sp->cell_begin;
+    for (int c = blockIdx.x * (kBigThreads / 32) + warp; c < nc; c += gridDim.x * (kBigThreads / 32)) {
+      const int b = start[c];
+      sort_cell(A.cell_atoms + Sp->atom_begin + b, start[c + 1] - b, buf, lane);
+    }
+  }
+}
+
+void launch_big_cells(const Arena& A, int64_t max_big_atoms, cudaStream_t st) {
+  if (max_big_atoms <= 0) return;
+  static bool attr = false;
+  const size_t smem = (size_t)(kBigThreads / 32) * kCellSortCap * sizeof(int);
+  if (!attr) {
+    cudaFuncSetAttribute(k_big_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr = true;
+  }
+  const unsigned atoms_blocks = (unsigned)std::min<int64_t>((max_big_atoms + kBigThreads - 1) / kBigThreads, 4096);
+  const unsigned cell_blocks = (unsigned)std::min<int64_t>((max_big_atoms / 2 + 8) / 8, 4096);  // cells <= atoms / 2
+  k_big_count<<<atoms_blocks, kBigThreads, 0, st>>>(A);
+  k_big_scan<<<1, 1024, 0, st>>>(A);
+  k_big_scatter<<<atoms_blocks, kBigThreads, 0, st>>>(A);
+  k_big_sort<<<cell_blocks, kBigThreads, smem, st>>>(A);
 }
 
 void launch_control_cells(const Arena& A, int n_sys, int mode, int nbr_override, cudaStream_t st) {

@@ -176,7 +176,8 @@ struct Arena {
   int* atom_cell = nullptr;
   // work list of 8-atom groups to (re)build; work_ctl[0] = queued groups
   int* work = nullptr;
-  int* work_ctl = nullptr;
+  int* work_ctl = nullptr;  // [0] queued groups, [1] systems in big_list
+  int* big_list = nullptr;  // rebuilding systems of >= kBigSortAtoms atoms (the control kernel appends)
   // systems
   SysDev* sys = nullptr;
   // FP64 batches only (null otherwise): the state and forces of the
@@ -202,6 +203,10 @@ constexpr int kIntBoth = 3;
 // launchers (nbr.cu, force.cu, integrate.cu)
 void launch_control_cells(const Arena& A, int n_sys, int mode, int nbr_mode_override,
                           cudaStream_t st);
+// Systems of at least this many atoms have their cells sorted by grid-wide
+// kernels (launch_big_cells) instead of inside their control block.
+constexpr int kBigSortAtoms = 16384;
+void launch_big_cells(const Arena& A, int64_t max_big_atoms, cudaStream_t st);
 // The per-system schedule decision of a step (one thread per system).
 void launch_decide(const Arena& A, int n_sys, cudaStream_t st);
 // Force launch selections.
