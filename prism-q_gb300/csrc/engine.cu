@@ -717,6 +717,8 @@ struct prismq_batch {
     for (auto& r : slots)
       if (r.fr_mem) cudaFree(r.fr_mem);
     if (gexec) cudaGraphExecDestroy(gexec);
+    if (gexec_head) cudaGraphExecDestroy(gexec_head);
+    if (gexec_tail) cudaGraphExecDestroy(gexec_tail);
     void* ptrs[] = {A.pos, A.vel, A.lj, A.xref, A.f, A.pe, A.atom_sys, A.mask_all, A.mask_ref, A.far,
                     A.far_list, A.inc, A.inc_list, A.ex_idx, A.ex_partner, A.ex_par, A.exc, A.grp, A.grp_refs, A.bonds, A.angles,
                     A.dihs, A.units, A.noise, A.nbr, A.nnbr, A.cell_start, A.cell_atoms, A.atom_cell, A.work, A.work_ctl, A.big_list, A.sys,
@@ -857,27 +859,44 @@ struct prismq_batch {
     return PRISMQ_OK;
   }
 
+  // Three graphs per batch shape: the head of a call (pre-force phases of its
+  // first step), the steady step, and the tail (the last step's forces and
+  // post-force phases), so that even a one-step call is two graph launches.
+  prismq_status capture(int part, cudaGraphExec_t* out) {
+    cudaGraph_t g;
+    PQ_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    prismq_status brc = PRISMQ_OK;
+    if (part == 0) {
+      integrate(kIntPre);
+    } else {
+      brc = enqueue_step_body();
+      integrate(part == 1 ? kIntBoth : kIntPost);
+    }
+    cudaError_t ce = cudaStreamEndCapture(st, &g);
+    if (brc != PRISMQ_OK) return brc;
+    PQ_CK(ce);
+    cudaError_t e = cudaGraphInstantiateWithFlags(out, g, cudaGraphInstantiateFlagUseNodePriority);
+    cudaGraphDestroy(g);
+    PQ_CK(e);
+    return PRISMQ_OK;
+  }
+
   prismq_status ensure_graph() {
     prismq_status trc = tune_force();
     if (trc != PRISMQ_OK) return trc;
     if (!graph_dirty && gexec) return PRISMQ_OK;
-    if (gexec) {
-      cudaGraphExecDestroy(gexec);
-      gexec = nullptr;
-    }
-    cudaGraph_t g;
-    PQ_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    prismq_status brc = enqueue_step_body();
-    integrate(kIntBoth);
-    cudaError_t ce = cudaStreamEndCapture(st, &g);
-    if (brc != PRISMQ_OK) return brc;
-    PQ_CK(ce);
-    cudaError_t e = cudaGraphInstantiateWithFlags(&gexec, g, cudaGraphInstantiateFlagUseNodePriority);
-    cudaGraphDestroy(g);
-    PQ_CK(e);
+    for (cudaGraphExec_t* g : {&gexec, &gexec_head, &gexec_tail})
+      if (*g) {
+        cudaGraphExecDestroy(*g);
+        *g = nullptr;
+      }
+    if ((trc = capture(1, &gexec)) != PRISMQ_OK) return trc;
+    if ((trc = capture(0, &gexec_head)) != PRISMQ_OK) return trc;
+    if ((trc = capture(2, &gexec_tail)) != PRISMQ_OK) return trc;
     graph_dirty = false;
     return PRISMQ_OK;
   }
+  cudaGraphExec_t gexec_head = nullptr, gexec_tail = nullptr;
 
   prismq_status prime_if_needed() {
     bool any = false;
@@ -1048,14 +1067,11 @@ struct prismq_batch {
     if (rc != PRISMQ_OK) return rc;
     rc = ensure_graph();
     if (rc != PRISMQ_OK) return rc;
-    g_launches += integrate(kIntPre);
     const int per_step = body_launches() + integrate_passes();
-    for (int64_t i = 1; i < n; ++i) {
-      PQ_CK(cudaGraphLaunch(gexec, st));
-      g_launches += per_step;
-    }
-    if ((rc = enqueue_step_body()) != PRISMQ_OK) return rc;
-    g_launches += body_launches() + integrate(kIntPost);
+    PQ_CK(cudaGraphLaunch(gexec_head, st));
+    for (int64_t i = 1; i < n; ++i) PQ_CK(cudaGraphLaunch(gexec, st));
+    PQ_CK(cudaGraphLaunch(gexec_tail, st));
+    g_launches += (int64_t)per_step * n + integrate_passes();  // head: the noise and integrate launches once more
     PQ_CK(cudaGetLastError());
     return check_status();
   }
