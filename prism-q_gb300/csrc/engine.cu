@@ -11,9 +11,12 @@
 //   fixed reference grid from the initial bounding box       :12285-12330
 //   Maxwell–Boltzmann start velocities with COM removed      :16065-16100
 //
-// One step on the device is four launches, captured once per batch shape in a
-// CUDA graph:  control+cells (per system) → neighbour rows → forces →
-// integrate (post-phases of this step fused with pre-phases of the next).
+// One step on the device, captured once per batch shape in a CUDA graph:
+// the schedule decision (per system) → [control+cells of the rebuilding
+// systems → their neighbour rows → their forces] beside [the forces of the
+// other systems on a second stream] → the OU normals → integrate (post-phases
+// of this step fused with pre-phases of the next).  Systems of 16k+ atoms
+// add four grid-wide cell-sort launches after the control kernel.
 #include <cuda_runtime.h>
 #include <nvtx3/nvToolsExt.h>
 
