@@ -2,7 +2,7 @@
 
 * neighbour scheme: golden vectors generated by scripts/physics_refs/neighbor_list.py
   (cell_pairs / brute_pairs) — synthetic_600 must give 94,216 brute-force pairs,
-  93,912 kept and 304 missed, none within 10 Å (SURVEY of the reference, REVIEW_BUNDLE
+  93,912 kept and 304 missed, none within 10 Å (the reference's REVIEW_BUNDLE.md,
   D-NBL-MISS-10-12);
 * Philox4x32-10 Random123 known-answer vectors (rng_streams.py:87-92);
 * the 418.4 half-kick (fused_engine.rs:4723-4731);

@@ -45,7 +45,7 @@ def test_polyala_term_counts(pq, nres):
     t = pq.Topology.polyala(1, nres, seed=5)
     n = 10 * nres
     assert t.n_atoms == n
-    assert len(t.bonds) == 10 * nres - 1           # SURVEY: bonds 10R-1
+    assert len(t.bonds) == 10 * nres - 1           # bonds 10R-1
     assert len(t.angles) == 18 * nres - 4          # angles 18R-4
     assert len(t.clusters) == 3 * nres             # NH, CH, CH3 per residue
     assert sum(int(c["n_hydrogens"]) for c in t.clusters) == 5 * nres
