@@ -285,15 +285,19 @@ prismq_status prismq_get_step_params(prismq_system* sys, float out[3]);
  * fingerprint and a payload checksum); restore refuses a blob of another
  * topology, size or library version, and a damaged one.  FP32 systems. */
 prismq_status prismq_checkpoint_size(prismq_system* sys, size_t* bytes);
+/* The same size for a system of n_atoms atoms (host only: sizes a buffer
+ * before the system exists, e.g. a served job's snapshot_out). */
+prismq_status prismq_checkpoint_size_for_atoms(int64_t n_atoms, size_t* bytes);
 prismq_status prismq_checkpoint_save(prismq_system* sys, void* buf, size_t cap, size_t* written);
 prismq_status prismq_checkpoint_restore(prismq_system* sys, const void* buf, size_t len);
 
 /* ---- trajectory frames (the reference records none: D-FRAMES-NOT-CAPTURED) ----
  *
- * Every `interval` steps the step graph writes the state at that step
- * boundary (positions after the step's drift and SHAKE, velocities after its
- * post-force phases; the values prismq_get_positions / get_velocities return
- * there) into a device ring of `capacity` frames, with no extra launch.
+ * Every `interval` steps the state at that step boundary (positions after the
+ * step's drift and SHAKE, velocities after its post-force phases; the values
+ * prismq_get_positions / get_velocities return there) is copied device to
+ * device into a ring of `capacity` frames: a step() call runs in segments
+ * that end on the frame boundaries, which changes no result.
  * interval 0 stops recording and frees the ring.  prismq_frames_read copies
  * out, oldest first, up to max_frames frames not yet read: AoS float[3N] per
  * frame into xyz (and vxyz when velocities were requested; may be NULL), the
@@ -427,6 +431,13 @@ int32_t prismq_batch_resident_systems(const prismq_batch* b);
  * topology and params, never on which other jobs share the GPU: results are
  * bit-identical to running the job alone.
  *
+ * Snapshots: a job may start from a checkpoint (resume: the bytes of
+ * prismq_checkpoint_save or of another job's snapshot, same topology) and may
+ * ask for its final checkpoint (snapshot_out, snapshot_cap >=
+ * prismq_checkpoint_size_for_atoms).  A long run split into jobs chained
+ * through snapshots is bit-identical to the run in one job; a job refused
+ * at restore fails with the restore's status and message.
+ *
  * Threading: every prismq_server_* call is internally locked and may come
  * from any thread. */
 
@@ -447,6 +458,10 @@ typedef struct prismq_job {
   float* velocities_out;           /* host float[3N] or NULL: final velocities */
   uint64_t tag;                    /* echoed in the result */
   const struct prismq_protocol* protocol; /* NULL: constant T, γ, dt; else copied by submit */
+  const void* resume;              /* NULL, or a checkpoint of this topology to start from (copied by submit) */
+  size_t resume_len;
+  void* snapshot_out;              /* NULL, or a host buffer for the job's final checkpoint */
+  size_t snapshot_cap;             /* its size (prismq_checkpoint_size of the system) */
 } prismq_job;
 
 typedef struct prismq_job_result {
@@ -459,6 +474,7 @@ typedef struct prismq_job_result {
   double start_s;   /* admission into the arena */
   double end_s;     /* results written to the job's buffers */
   char message[160];
+  uint64_t snapshot_len;  /* bytes written to snapshot_out (0: none requested, or the job failed) */
 } prismq_job_result;
 
 typedef struct prismq_server_stats {

@@ -114,13 +114,16 @@ class ServerConfigStruct(ctypes.Structure):
 
 class JobStruct(ctypes.Structure):
     _fields_ = [("topology", _P), ("params", ParamsStruct), ("n_steps", ctypes.c_int64),
-                ("positions_out", _P), ("velocities_out", _P), ("tag", ctypes.c_uint64), ("protocol", _P)]
+                ("positions_out", _P), ("velocities_out", _P), ("tag", ctypes.c_uint64), ("protocol", _P),
+                ("resume", _P), ("resume_len", ctypes.c_size_t), ("snapshot_out", _P),
+                ("snapshot_cap", ctypes.c_size_t)]
 
 
 class JobResultStruct(ctypes.Structure):
     _fields_ = [("job_id", ctypes.c_int64), ("tag", ctypes.c_uint64), ("status", ctypes.c_int),
                 ("n_atoms", ctypes.c_int32), ("steps_done", ctypes.c_int64), ("submit_s", ctypes.c_double),
-                ("start_s", ctypes.c_double), ("end_s", ctypes.c_double), ("message", ctypes.c_char * 160)]
+                ("start_s", ctypes.c_double), ("end_s", ctypes.c_double), ("message", ctypes.c_char * 160),
+                ("snapshot_len", ctypes.c_uint64)]
 
 
 class ServerStatsStruct(ctypes.Structure):
@@ -167,6 +170,7 @@ def load() -> ctypes.CDLL:
         "prismq_batch_set_protocol": (I, [P, ctypes.c_int32, P]),
         "prismq_batch_get_step_params": (I, [P, ctypes.c_int32, P]),
         "prismq_checkpoint_size": (I, [P, P]),
+        "prismq_checkpoint_size_for_atoms": (I, [ctypes.c_int64, P]),
         "prismq_checkpoint_save": (I, [P, P, ctypes.c_size_t, P]),
         "prismq_checkpoint_restore": (I, [P, P, ctypes.c_size_t]),
         "prismq_batch_checkpoint_size": (I, [P, ctypes.c_int32, P]),
@@ -777,6 +781,7 @@ class JobResult:
     message: str
     positions: np.ndarray | None
     velocities: np.ndarray | None
+    snapshot: bytes | None = None
 
     @property
     def latency_s(self) -> float:
@@ -818,18 +823,31 @@ class Server:
         self.close()
 
     def submit(self, topology: Topology, n_steps: int, params: Params | None = None, tag: int = 0,
-               want_state: bool = True, protocol: "Protocol | None" = None) -> int:
+               want_state: bool = True, protocol: "Protocol | None" = None, resume: bytes | None = None,
+               want_snapshot: bool = False) -> int:
+        """Queue a job.  ``resume`` is a checkpoint of this topology to start
+        from (a job's snapshot or an engine's checkpoint); ``want_snapshot``
+        returns the job's final checkpoint in ``JobResult.snapshot``."""
         n = topology.n_atoms
         x = np.zeros((n, 3), np.float32) if want_state else None
         v = np.zeros((n, 3), np.float32) if want_state else None
         t = topology.struct()
         ps = protocol.struct() if protocol is not None else None
+        snap = None
+        if want_snapshot:
+            size = ctypes.c_size_t()
+            _check(load().prismq_checkpoint_size_for_atoms(int(n), ctypes.byref(size)))
+            snap = ctypes.create_string_buffer(size.value)
+        rb = bytes(resume) if resume is not None else None
         job = JobStruct(ctypes.cast(ctypes.pointer(t), _P), (params or Params()).struct(), int(n_steps),
                         _ptr(x), _ptr(v), int(tag) & 0xffffffffffffffff,
-                        ctypes.cast(ctypes.pointer(ps), _P) if ps is not None else None)
+                        ctypes.cast(ctypes.pointer(ps), _P) if ps is not None else None,
+                        ctypes.cast(ctypes.c_char_p(rb), _P) if rb else None, len(rb) if rb else 0,
+                        ctypes.cast(snap, _P) if snap is not None else None,
+                        ctypes.sizeof(snap) if snap is not None else 0)
         jid = ctypes.c_int64()
         _check(load().prismq_server_submit(self.h, ctypes.byref(job), ctypes.byref(jid)))
-        self._out[jid.value] = (x, v)  # the worker writes here when the job ends
+        self._out[jid.value] = (x, v, snap)  # the worker writes here when the job ends
         return jid.value
 
     def poll(self, wait_ms: int = 0, max_results: int = 256) -> list[JobResult]:
@@ -838,9 +856,10 @@ class Server:
         _check(load().prismq_server_poll(self.h, buf, max_results, ctypes.byref(n), int(wait_ms)))
         out = []
         for r in buf[:n.value]:
-            x, v = self._out.pop(r.job_id, (None, None))
+            x, v, snap = self._out.pop(r.job_id, (None, None, None))
+            blob = snap.raw[:r.snapshot_len] if snap is not None and r.snapshot_len else None
             out.append(JobResult(r.job_id, r.tag, r.status, r.n_atoms, r.steps_done, r.submit_s, r.start_s,
-                                 r.end_s, r.message.decode(errors="replace"), x, v))
+                                 r.end_s, r.message.decode(errors="replace"), x, v, blob))
         return out
 
     def stats(self) -> dict:

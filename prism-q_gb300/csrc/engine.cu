@@ -2311,6 +2311,12 @@ prismq_status prismq_frames_read(prismq_system* sys, float* xyz, float* vxyz, in
   return prismq_batch_frames_read(sys->b, sys->slot, xyz, vxyz, steps, max_frames, n_out, dropped);
 }
 
+prismq_status prismq_checkpoint_size_for_atoms(int64_t n_atoms, size_t* bytes) {
+  if (!bytes || n_atoms < 0) return fail(PRISMQ_E_INVALID, "n_atoms < 0 or bytes NULL");
+  *bytes = ckpt_bytes(n_atoms);
+  return PRISMQ_OK;
+}
+
 prismq_status prismq_checkpoint_size(prismq_system* sys, size_t* bytes) {
   if (!sys) return fail(PRISMQ_E_INVALID, "system is NULL");
   return prismq_batch_checkpoint_size(sys->b, sys->slot, bytes);

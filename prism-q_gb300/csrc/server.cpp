@@ -47,8 +47,12 @@ struct Job {
   float* vout = nullptr;
   double t_submit = 0.0, t_start = 0.0;
   int32_t slot = -1;
+  int64_t step0 = 0;  // the system's step counter at admission (a resumed job's start)
   bool has_protocol = false;
   prismq_protocol protocol{};
+  std::vector<char> resume;  // checkpoint to start from (empty: the topology's own state)
+  void* snap = nullptr;      // where the final checkpoint goes
+  size_t snap_cap = 0;
 };
 
 void copy_message(char* dst, size_t cap, const std::string& msg) {
@@ -106,15 +110,25 @@ struct prismq_server {
       lk.unlock();
       int32_t slot = -1;
       prismq_status rc = pq::admit_prepared(batch, prep, &slot);
-      if (rc == PRISMQ_OK && j.has_protocol && (rc = prismq_batch_set_protocol(batch, slot, &j.protocol)) != PRISMQ_OK)
-        prismq_batch_remove_system(batch, slot);
+      const bool admitted = rc == PRISMQ_OK;
+      if (rc == PRISMQ_OK && !j.resume.empty())
+        rc = prismq_batch_checkpoint_restore(batch, slot, j.resume.data(), j.resume.size());
+      int64_t step0 = 0;
+      if (rc == PRISMQ_OK && !j.resume.empty()) rc = prismq_batch_get_step(batch, slot, &step0);
+      if (rc == PRISMQ_OK && j.has_protocol) rc = prismq_batch_set_protocol(batch, slot, &j.protocol);
       const std::string msg = rc != PRISMQ_OK ? prismq_last_error() : "";
+      if (admitted && rc != PRISMQ_OK) {
+        prismq_batch_remove_system(batch, slot);
+        if (rc == PRISMQ_E_CAPACITY) rc = PRISMQ_E_INVALID;  // only admission may defer a job
+      }
       lk.lock();
       if (rc == PRISMQ_OK) {
         j.slot = slot;
         j.t_start = now();
+        j.step0 = step0;
         pq::free_prepared(j.prep);  // uploaded; the host copy is no longer needed
         j.prep = nullptr;
+        std::vector<char>().swap(j.resume);
         resident.push_back(j);
         it = queue.erase(it);
         continue;
@@ -172,15 +186,22 @@ struct prismq_server {
           }
           js = prismq_batch_get_state(batch, j.slot, j.xout, j.vout);
           if (js != PRISMQ_OK) msg = prismq_last_error();
+          if (js == PRISMQ_OK && j.snap) {
+            size_t written = 0;
+            js = prismq_batch_checkpoint_save(batch, j.slot, j.snap, j.snap_cap, &written);
+            if (js != PRISMQ_OK) msg = prismq_last_error();
+            j.snap_cap = js == PRISMQ_OK ? written : 0;
+          }
         }
         int64_t steps_done = j.n_steps;
         if (js != PRISMQ_OK) {
           int64_t s = 0;
-          steps_done = prismq_batch_get_step(batch, j.slot, &s) == PRISMQ_OK ? s : j.n_steps - j.remaining;
+          steps_done = prismq_batch_get_step(batch, j.slot, &s) == PRISMQ_OK ? s - j.step0 : j.n_steps - j.remaining;
           if (msg.empty()) msg = step_msg;
         }
         prismq_batch_remove_system(batch, j.slot);
         done.push_back(make_result(j, js, steps_done, msg));
+        done.back().snapshot_len = js == PRISMQ_OK && j.snap ? j.snap_cap : 0;
         (js == PRISMQ_OK ? completed : failed) += 1;
       }
       lk.lock();
@@ -271,6 +292,13 @@ prismq_status prismq_server_submit(prismq_server* s, const prismq_job* job, int6
                        std::to_string(s->capacity_atoms));
     return PRISMQ_E_CAPACITY;
   }
+  size_t ckpt = 0;
+  prismq_checkpoint_size_for_atoms(n, &ckpt);
+  if ((job->snapshot_out && job->snapshot_cap < ckpt) || (job->resume && job->resume_len != ckpt)) {
+    pq::free_prepared(prep);  // the blob's own checks run at admission; its size is known now
+    pq::set_last_error("snapshot buffer or resume blob is not " + std::to_string(ckpt) + " bytes");
+    return PRISMQ_E_INVALID;
+  }
   Job j;
   j.tag = job->tag;
   j.prep = prep;
@@ -282,6 +310,12 @@ prismq_status prismq_server_submit(prismq_server* s, const prismq_job* job, int6
     j.has_protocol = true;
     j.protocol = *job->protocol;
   }
+  if (job->resume && job->resume_len > 0) {
+    const char* r = static_cast<const char*>(job->resume);
+    j.resume.assign(r, r + job->resume_len);
+  }
+  j.snap = job->snapshot_out;
+  j.snap_cap = job->snapshot_out ? job->snapshot_cap : 0;
   {
     std::lock_guard<std::mutex> g(s->mu);
     j.id = s->next_id++;

@@ -38,9 +38,9 @@ def test_server_structs_match_the_header(pq):
     # sizes of the C structs on LP64 (x86-64 and aarch64): the ctypes mirrors
     # must agree or every field after the first mismatch is misread
     assert ctypes.sizeof(pq.ServerConfigStruct) == 16
-    assert ctypes.sizeof(pq.JobStruct) == 104
+    assert ctypes.sizeof(pq.JobStruct) == 136
     assert ctypes.sizeof(pq.ParamsStruct) == 56
-    assert ctypes.sizeof(pq.JobResultStruct) == 216
+    assert ctypes.sizeof(pq.JobResultStruct) == 224
     assert ctypes.sizeof(pq.ServerStatsStruct) == 96
 
 
@@ -190,3 +190,50 @@ def test_invalid_protocol_rejected_at_submit(gpu, mix):
     with gpu.Server(1 << 28) as srv:
         with pytest.raises(gpu.PrismQError):
             srv.submit(mix[0][0], 10, mix[0][1], protocol=bad)
+
+
+@pytest.mark.gpu
+def test_job_chain_through_snapshots_equals_one_job(gpu, mix):
+    """A 1000-step run split into three served jobs chained by snapshots
+    (one of them resumed from an engine's checkpoint) equals the run alone;
+    other jobs share the arena meanwhile."""
+    t, p, _ = mix[1]
+    ref = _alone(gpu, t, p, 1000)
+    with gpu.Server(1 << 30, chunk_steps=64) as srv:
+        side = srv.submit(mix[0][0], 300, mix[0][1])
+        a = srv.submit(t, 400, p, want_snapshot=True)
+        res = _drain(srv, 2)
+        assert res[a].ok and res[side].ok and res[a].snapshot is not None
+        e = gpu.NhsAmberFusedEngine(t, gpu.Params(stream=999))
+        e.restore(res[a].snapshot)
+        assert e.timestep == 400
+        e.step(250)
+        b = srv.submit(t, 350, gpu.Params(stream=5), resume=e.checkpoint(), want_snapshot=True)
+        rb = _drain(srv, 1)[b]
+        e.close()
+    assert rb.ok, rb.message
+    assert np.array_equal(rb.positions, ref[0]) and np.array_equal(rb.velocities, ref[1])
+    f = gpu.NhsAmberFusedEngine(t, gpu.Params())
+    f.restore(rb.snapshot)
+    assert f.timestep == 1000
+    assert np.array_equal(f.get_positions(), ref[0]) and np.array_equal(f.get_velocities(), ref[1])
+    f.close()
+
+
+@pytest.mark.gpu
+def test_bad_resume_fails_the_job_alone(gpu, mix, ala40):
+    e = gpu.NhsAmberFusedEngine(ala40, gpu.Params())
+    e.step(3)
+    blob = bytearray(e.checkpoint())
+    e.close()
+    blob[-3] ^= 0x01
+    t, p, n = mix[0]
+    ref = _alone(gpu, t, p, n)
+    with gpu.Server(1 << 30, chunk_steps=40) as srv:
+        with pytest.raises(gpu.PrismQError):
+            srv.submit(ala40, 10, resume=bytes(blob[:-1]))  # wrong size: refused at submit
+        bad = srv.submit(ala40, 10, resume=bytes(blob))
+        good = srv.submit(t, n, p)
+        res = _drain(srv, 2)
+    assert not res[bad].ok and "corrupted" in res[bad].message and res[bad].steps_done == 0
+    assert res[good].ok and np.array_equal(res[good].positions, ref[0])
