@@ -388,6 +388,10 @@ prismq_status prismq_batch_frames_read(prismq_batch* b, int32_t slot, float* xyz
  * resident blocks per SM given to the register allocator.  The launch shape
  * does not change results. */
 prismq_status prismq_batch_tuning(prismq_batch* b, int32_t out[3]);
+/* Pin the force kernel's launch shape to `variant` (0 .. n-1; *n_variants
+ * receives n, may be NULL), or hand the choice back to the autotuner with
+ * variant -1.  Every shape gives the same bits. */
+prismq_status prismq_batch_set_force_variant(prismq_batch* b, int32_t variant, int32_t* n_variants);
 /* out[0] = steps taken, out[1] = neighbour-list builds so far. */
 prismq_status prismq_batch_counters(prismq_batch* b, int32_t slot, int64_t out[2]);
 prismq_status prismq_batch_energy(prismq_batch* b, int32_t slot, double out[6]);

@@ -222,6 +222,7 @@ def load() -> ctypes.CDLL:
         "prismq_batch_time_force": (I, [P, ctypes.c_int32, P]),
         "prismq_batch_counters": (I, [P, ctypes.c_int32, P]),
         "prismq_batch_tuning": (I, [P, P]),
+        "prismq_batch_set_force_variant": (I, [P, ctypes.c_int32, P]),
         "prismq_batch_create_ex": (I, [i64, ctypes.c_int32, ctypes.c_int32, P]),
         "prismq_batch_virial": (I, [P, ctypes.c_int32, P]),
         "prismq_batch_get_state_f64": (I, [P, ctypes.c_int32, P, P]),
@@ -727,6 +728,12 @@ class Batch:
         out = np.zeros(3, np.int32)
         _check(load().prismq_batch_tuning(self.h, _ptr(out)))
         return {"variant": int(out[0]), "block": int(out[1]), "min_blocks_per_sm": int(out[2])}
+
+    def set_force_variant(self, variant: int) -> int:
+        """Pin the force kernel's launch shape (-1: autotune); returns the number of shapes."""
+        n = ctypes.c_int32()
+        _check(load().prismq_batch_set_force_variant(self.h, int(variant), ctypes.byref(n)))
+        return n.value
 
     def counters(self, slot: int) -> tuple[int, int]:
         """(steps taken, neighbour-list builds) of one system."""

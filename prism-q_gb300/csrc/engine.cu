@@ -700,6 +700,7 @@ struct prismq_batch {
   int64_t atom_span = 0, unit_span = 0;
   int sys_span = 0;
   int force_variant = -1;  // autotuned launch shape of the force kernel
+  bool force_pinned = false;  // set by prismq_batch_set_force_variant: no re-tuning
   int64_t tuned_span = -1;
   double* d_energy = nullptr;  // kEnergyOut per system
   float* d_stage = nullptr;
@@ -834,6 +835,7 @@ struct prismq_batch {
   prismq_status tune_force() {
     // re-tune only when the resident span has changed by 2x or more since the
     // last tuning, so that admission churn in a server does not re-time shapes
+    if (force_pinned) return PRISMQ_OK;
     if (force_variant >= 0 && atom_span <= 2 * tuned_span && 2 * atom_span >= tuned_span) return PRISMQ_OK;
     cudaEvent_t e0, e1;
     PQ_CK(cudaEventCreate(&e0));
@@ -1612,6 +1614,17 @@ prismq_status prismq_batch_get_step(prismq_batch* b, int32_t slot, int64_t* step
   rc = b->sync_sys_from_device();
   if (rc != PRISMQ_OK) return rc;
   *step = b->h_sys[slot].step;
+  return PRISMQ_OK;
+}
+
+prismq_status prismq_batch_set_force_variant(prismq_batch* b, int32_t variant, int32_t* n_variants) {
+  if (!b) return fail(PRISMQ_E_INVALID, "batch is NULL");
+  if (n_variants) *n_variants = force_variant_count();
+  if (variant < -1 || variant >= force_variant_count()) return fail(PRISMQ_E_INVALID, "no such force variant");
+  if (variant != b->force_variant) b->graph_dirty = true;
+  b->force_pinned = variant >= 0;
+  b->force_variant = variant;
+  b->tuned_span = 0;
   return PRISMQ_OK;
 }
 

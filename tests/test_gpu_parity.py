@@ -221,6 +221,29 @@ def test_repeat_runs_are_bit_identical(gpu, ala250):
     b.close()
 
 
+def test_every_force_launch_shape_gives_the_same_bits(gpu):
+    """The autotuner's launch shapes (registers per thread) change speed
+    only: 45 steps of a mixed batch, across list rebuilds, end in the same
+    bits under each shape."""
+    topos = [gpu.Topology.polyala(1, n, seed=30 + n) for n in (7, 45, 130)]
+    states, shapes = [], []
+    n_shapes = 1
+    v = 0
+    while v < n_shapes:
+        b = gpu.Batch(max_atoms=2048, max_systems=4)
+        slots = [b.add_system(t, gpu.Params(stream=k)) for k, t in enumerate(topos)]
+        n_shapes = b.set_force_variant(v)
+        b.step(45)
+        states.append([b.get_state(s) for s in slots])
+        shapes.append(b.tuning())
+        b.close()
+        v += 1
+    assert n_shapes >= 2 and len({s["min_blocks_per_sm"] for s in shapes}) == n_shapes
+    for other in states[1:]:
+        for (x0, v0), (x1, v1) in zip(states[0], other):
+            assert np.array_equal(x0, x1) and np.array_equal(v0, v1)
+
+
 def test_constraints_hold_along_the_trajectory(gpu, ala250):
     eng = gpu.NhsAmberFusedEngine(ala250, gpu.Params())
     for _ in range(5):
