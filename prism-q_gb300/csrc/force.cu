@@ -540,7 +540,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_force(Arena A, int64_t n_sp
   const R2<R> li = ljp[a];
   const R qi = pi.w;
   const int n = A.nnbr[a];
-  const int* row = A.nbr + nbr_index(a, q);  // entry 4t+q is at row[32 t]
+  const int* row = A.nbr + nbr_index(a, q);  // entry 4t+q is at row[128 (t/4) + t%4]
   R inv_rc = R(0.0f);
   if (kEnergy) inv_rc = inv_sqrt_r(cut2);
   const int mine = n > q ? (n - q + kLanes - 1) / kLanes : 0;
@@ -550,23 +550,17 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_force(Arena A, int64_t n_sp
     // branch, so a lane keeps several gathers in flight and lanes never
     // diverge.  Pairs outside the cutoff contribute an exact zero, so the sum
     // is the same sequence of additions as a branching loop.
-    // The row indices of the next four entries are loaded while the current
-    // four are gathered and evaluated.  Partial sums flush after every 32 of
-    // the lane's entries, as in a loop over 32-entry chunks.
+    // The row indices of the next four entries (one int4) are loaded while
+    // the current four are gathered and evaluated.  Partial sums flush after
+    // every 32 of the lane's entries, as in a loop over 32-entry chunks.
     const int m4 = mine & ~3;
-    int jn[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) jn[u] = m4 > 0 ? __ldg(row + (int64_t)u * 32) : 0;
+    const int4* row4 = reinterpret_cast<const int4*>(row);  // block t/4 of the lane at row4[32 (t/4)]
+    int4 jn = m4 > 0 ? __ldg(row4) : make_int4(0, 0, 0, 0);
     for (int t = 0; t < m4; t += 4) {
-      int j[4];
+      const int j[4] = {jn.x, jn.y, jn.z, jn.w};
       R4<R> pj[4];
       R2<R> lj[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) j[u] = jn[u];
-      if (t + 4 < m4) {
-#pragma unroll
-        for (int u = 0; u < 4; ++u) jn[u] = __ldg(row + (int64_t)(t + 4 + u) * 32);
-      }
+      if (t + 4 < m4) jn = __ldg(row4 + (int64_t)(t + 4) * 8);
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
         pj[u] = ldg_r4(pos + j[u]);
@@ -577,7 +571,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_force(Arena A, int64_t n_sp
       if (((t + 4) & 31) == 0) f.flush();
     }
     for (int t = m4; t < mine; ++t) {
-      const int j = __ldg(row + (int64_t)t * 32);
+      const int j = __ldg(row + (int64_t)(t >> 2) * 128 + (t & 3));
       pair_accumulate<R>(pi, qi, li, ldg_r4(pos + j), __ldg(ljp + j), cut2, f);
     }
     f.flush();
@@ -586,7 +580,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_force(Arena A, int64_t n_sp
       const int t1 = min(mine, t0 + 32);
 #pragma unroll 4
       for (int t = t0; t < t1; ++t) {
-        const int j = __ldg(row + (int64_t)t * 32);
+        const int j = __ldg(row + (int64_t)(t >> 2) * 128 + (t & 3));
         const R4<R> pj = ldg_r4(pos + j);
         const R dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
         const R r2 = fma_r(dz, dz, fma_r(dy, dy, dx * dx));

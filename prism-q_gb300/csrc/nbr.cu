@@ -642,7 +642,7 @@ __device__ __forceinline__ void group_test(const Arena& A, const GroupShared& sh
     } else {
       if (keep) {
         const int k = cnt[i] + __popc(bal & lt);  // same slot as nbr_index(ai, k)
-        rows[(k & ~3) * 8 + (i << 2) + (k & 3)] = j;
+        rows[(k >> 4) * 128 + (((i << 2) + (k & 3)) << 2) + ((k >> 2) & 3)] = j;
       }
       cnt[i] += add;
     }

@@ -17,11 +17,14 @@ namespace pq {
 constexpr int kNbrCap = 1024;     // neighbour row capacity per atom
 constexpr int kLanes = 4;         // threads per atom in the force kernel (fixed: results depend on it)
 
-// Row storage is tiled for the force kernel's warp shape (8 atoms x 4 lanes):
-// entry k of atom a lives at group (a/8), line k/4, slot (a%8)*4 + k%4, so a
-// warp's 32 index loads for one iteration are one contiguous 128-byte line.
+// Row storage is tiled for the force kernel's warp shape (8 atoms x 4 lanes;
+// lane q of atom a takes entries k = 4t + q).  Each lane's entries t..t+3
+// (t a multiple of 4) are one aligned int4, and the 32 lanes' int4s of an
+// 8-atom group are one contiguous 512-byte block:
+//   group a/8, block t/4, lane slot (a%8)*4 + q, word t%4.
 __host__ __device__ __forceinline__ int64_t nbr_index(int64_t a, int k) {
-  return ((a >> 3) * kNbrCap + (k & ~3)) * 8 + ((a & 7) << 2) + (k & 3);
+  const int t = k >> 2;
+  return (a >> 3) * (kNbrCap * 8) + (t >> 2) * 128 + ((((int)(a & 7) << 2) + (k & 3)) << 2) + (t & 3);
 }
 constexpr int kRefCellCap = 512;  // REF27 cell capacity (MAX_ATOMS_PER_CELL)
 constexpr int kRefMaxDim = 32;    // REF27 cells per axis (MAX_CELLS_PER_DIM)
