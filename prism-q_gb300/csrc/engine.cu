@@ -676,6 +676,7 @@ struct SlotRec {
   int64_t inc_b = 0, n_inc = 0, ex_b = 0, n_ex = 0, far_b = 0, n_far = 0, cell_b = 0, n_cell = 0;
   int64_t exc_b = 0, n_exc = 0, gref_b = 0, n_gref = 0;
   int max_group_slots = 0;
+  int32_t units_by_nh[4] = {0, 0, 0, 0};  // the slot's units hold 3, 2, 1, 0 hydrogens in this order
   bool ref_ok = false;
   bool need_prime = true;
   prismq_params params{};
@@ -725,7 +726,7 @@ struct prismq_batch {
     if (gexec_tail) cudaGraphExecDestroy(gexec_tail);
     void* ptrs[] = {A.pos, A.vel, A.lj, A.xref, A.f, A.pe, A.atom_sys, A.mask_all, A.mask_ref, A.far,
                     A.far_list, A.inc, A.inc_list, A.ex_idx, A.ex_partner, A.ex_par, A.exc, A.grp, A.grp_refs, A.bonds, A.angles,
-                    A.dihs, A.units, A.noise, A.nbr, A.nnbr, A.cell_start, A.cell_atoms, A.atom_cell, A.work, A.work_ctl, A.big_list, A.sys,
+                    A.dihs, A.units, A.unit_order, A.noise, A.nbr, A.nnbr, A.cell_start, A.cell_atoms, A.atom_cell, A.work, A.work_ctl, A.big_list, A.sys,
                     A.pos64, A.vel64, A.f64, A.lj64, d_energy, d_stage, d_stage2, d_stage64};
     for (void* p : ptrs)
       if (p) cudaFree(p);
@@ -739,6 +740,29 @@ struct prismq_batch {
   void control(int mode, int nbr_override, cudaStream_t s) {
     launch_control_cells(A, sys_span, mode, nbr_override, s);
     launch_big_cells(A, max_big_atoms, s);
+  }
+
+  // Integrate order: the units of every resident system with three
+  // hydrogens, then two, one and none.  The integrate grid walks this list,
+  // so the longest constraint chains start in the first wave of blocks and
+  // the short ones fill in behind them.  Each unit is still integrated once,
+  // by the same code, so the order changes no result.
+  std::vector<int> h_order;
+  int64_t n_order = 0;
+  prismq_status upload_order() {
+    h_order.clear();
+    for (int nh = 3; nh >= 0; --nh)
+      for (const SlotRec& R : slots) {
+        if (!R.active) continue;
+        int64_t b = R.unit_b;
+        for (int k = 3; k > nh; --k) b += R.units_by_nh[3 - k];
+        for (int32_t i = 0; i < R.units_by_nh[3 - nh]; ++i) h_order.push_back((int)(b + i));
+      }
+    if ((int64_t)h_order.size() != n_order) graph_dirty = true;
+    n_order = (int64_t)h_order.size();
+    if (n_order > 0)
+      PQ_CK(cudaMemcpyAsync(A.unit_order, h_order.data(), sizeof(int) * h_order.size(), cudaMemcpyHostToDevice, st));
+    return PRISMQ_OK;
   }
 
   void update_spans() {
@@ -780,16 +804,16 @@ struct prismq_batch {
   int integrate(int mode) {
     launch_noise(A, atom_span, mode, st);
     if (A.fp64) {
-      launch_integrate(A, unit_span, mode, st, 0);
+      launch_integrate(A, n_order, mode, st, 0);
       return 2;
     }
     int k = 1;
     if (n_check32 > 0 || n_check64 == 0) {
-      launch_integrate(A, unit_span, mode, st, 0);
+      launch_integrate(A, n_order, mode, st, 0);
       ++k;
     }
     if (n_check64 > 0) {
-      launch_integrate(A, unit_span, mode, st, 1);
+      launch_integrate(A, n_order, mode, st, 1);
       ++k;
     }
     return k;
@@ -1153,6 +1177,7 @@ prismq_status batch_alloc(prismq_batch* B, int64_t atom_cap, int sys_cap, int64_
   PQ_ALLOC(A.angles, A.angle_cap);
   PQ_ALLOC(A.dihs, A.dih_cap);
   PQ_ALLOC(A.units, A.unit_cap);
+  PQ_ALLOC(A.unit_order, A.unit_cap);
   PQ_ALLOC(A.noise, 2 * atom_cap);
   PQ_ALLOC(A.nbr, (atom_cap / 32) * (int64_t)kNbrCap * 32);
   PQ_ALLOC(A.nnbr, atom_cap);
@@ -1337,6 +1362,9 @@ prismq_status batch_admit(prismq_batch* B, const Lowered& L0, const prismq_param
   PQ_UP(A.angles + R.angle_b, L.angles);
   PQ_UP(A.dihs + R.dih_b, L.dihs);
   PQ_UP(A.units + R.unit_b, L.units);
+  for (int k = 0; k < 4; ++k) R.units_by_nh[k] = 0;
+  for (const Unit& u : L.units)
+    if (u.nh >= 0 && u.nh <= 3) R.units_by_nh[3 - u.nh] += 1;
   PQ_UP(A.exc + R.exc_b, L.excs);
   PQ_UP(A.grp_refs + R.gref_b, L.grp_refs);
   PQ_UP(A.grp + ab / kForceGroup, L.grp);
@@ -1383,6 +1411,7 @@ prismq_status batch_admit(prismq_batch* B, const Lowered& L0, const prismq_param
   B->slots[slot] = R;
   B->h_sys[slot] = S;
   B->update_spans();
+  if ((rc = B->upload_order()) != PRISMQ_OK) return rc;
   *slot_out = slot;
   return PRISMQ_OK;
 }
@@ -1414,7 +1443,7 @@ prismq_status batch_release(prismq_batch* B, int slot) {
   B->r_gref.release(R.gref_b, R.n_gref);
   R = SlotRec();
   B->update_spans();
-  return PRISMQ_OK;
+  return B->upload_order();
 }
 
 prismq_status get_xyz(prismq_batch* B, int slot, float4* src_plane, float* out) {

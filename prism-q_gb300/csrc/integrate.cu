@@ -15,11 +15,13 @@ namespace pq {
 // R = float: the production step, for the systems whose constraint checks run
 // in FP32 (kCheck64 false) or FP64 (kCheck64 true); R = double: the
 // FP64-everywhere step of an FP64 batch.
+// The grid walks A.unit_order (n_units entries), so the units with the
+// longest constraint chains are scheduled first.
 template <class R, bool kCheck64>
 __global__ void __launch_bounds__(128, 8) k_integrate(Arena A, int64_t n_units, int mode) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_units) return;
-  const Unit U = A.units[t];
+  const Unit U = A.units[A.unit_order[t]];
   if (U.nh < 0) return;
   SysDev* Sp = &A.sys[U.sys];
   const SysDev S = *Sp;

@@ -166,8 +166,10 @@ struct Arena {
   BondT* bonds = nullptr;
   AngleT* angles = nullptr;
   DihT* dihs = nullptr;
-  // constraint units
+  // constraint units, and the order the integrate grid walks them in
+  // (indices into units: every system's 3-hydrogen units, then 2, 1, 0)
   Unit* units = nullptr;
+  int* unit_order = nullptr;
   // OU normals drawn ahead of the integrate launch, per atom: [0, atom_cap)
   // for post(s-1), [atom_cap, 2 atom_cap) for pre(s)
   float4* noise = nullptr;
