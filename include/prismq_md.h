@@ -403,7 +403,12 @@ int64_t prismq_batch_resident_atoms(const prismq_batch* b);
  * prismq_batch_atom_span; system `slot` starts at prismq_batch_atom_offset).
  * Entries of free arena ranges are ignored on upload.  Uploaded positions that
  * differ bitwise from the resident ones refresh that system's list and forces
- * before its next step. */
+ * before its next step.  Pinned (page-locked) host arrays are read and written
+ * by the transfer kernel directly over the host link; pageable arrays go
+ * through a device staging copy.  get_state_all returns with the arrays
+ * filled.  set_state_all is ordered before every later call on the batch;
+ * a pageable array may be reused when it returns, a pinned one once a later
+ * call that returns host data (get_state_all, ...) has returned. */
 int64_t prismq_batch_atom_span(const prismq_batch* b);
 int64_t prismq_batch_atom_offset(const prismq_batch* b, int32_t slot);
 prismq_status prismq_batch_set_state_all(prismq_batch* b, const float* xyz, const float* vxyz);

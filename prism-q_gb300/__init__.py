@@ -729,6 +729,34 @@ class Batch:
         _check(load().prismq_batch_tuning(self.h, _ptr(out)))
         return {"variant": int(out[0]), "block": int(out[1]), "min_blocks_per_sm": int(out[2])}
 
+    def atom_span(self) -> int:
+        """Length (atoms) of the whole-arena state arrays."""
+        return int(load().prismq_batch_atom_span(self.h))
+
+    def atom_offset(self, slot: int) -> int:
+        """First arena atom of a resident system."""
+        return int(load().prismq_batch_atom_offset(self.h, slot))
+
+    def get_state_all(self, xyz: np.ndarray | None = None, vxyz: np.ndarray | None = None):
+        """Fill float32 [3 * atom_span] arrays (pinned host memory is written
+        directly by the device; allocates pageable arrays when none are given)."""
+        n = 3 * self.atom_span()
+        if xyz is None and vxyz is None:
+            xyz, vxyz = np.empty(n, np.float32), np.empty(n, np.float32)
+        for a in (xyz, vxyz):
+            if a is not None and (a.dtype != np.float32 or a.size != n or not a.flags.c_contiguous):
+                raise ValueError(f"state arrays must be contiguous float32 of {n} values")
+        _check(load().prismq_batch_get_state_all(self.h, _ptr(xyz), _ptr(vxyz)))
+        return xyz, vxyz
+
+    def set_state_all(self, xyz: np.ndarray | None, vxyz: np.ndarray | None) -> None:
+        """Upload whole-arena state (float32 [3 * atom_span]; None leaves it)."""
+        n = 3 * self.atom_span()
+        for a in (xyz, vxyz):
+            if a is not None and (a.dtype != np.float32 or a.size != n or not a.flags.c_contiguous):
+                raise ValueError(f"state arrays must be contiguous float32 of {n} values")
+        _check(load().prismq_batch_set_state_all(self.h, _ptr(xyz), _ptr(vxyz)))
+
     def set_force_variant(self, variant: int) -> int:
         """Pin the force kernel's launch shape (-1: autotune); returns the number of shapes."""
         n = ctypes.c_int32()

@@ -621,17 +621,49 @@ __global__ void k_xyz_to_aos64(double* dst, const float4* src, int n) {
   dst[3 * i + 1] = v.y;
   dst[3 * i + 2] = v.z;
 }
-// Whole-arena state upload: positions whose bits change mark their system for
-// a force/list refresh before the next step.
-__global__ void k_set_state_all(float4* pos, float4* vel, double4_32a* pos64, double4_32a* vel64, const float* xs,
-                                const float* vs, const int* atom_sys, SysDev* sys, int64_t n) {
-  const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (a >= n) return;
+// Whole-arena state transfer, 256 atoms per block.  The block's AoS segment
+// (3072 bytes per array) moves through shared memory as 16-byte vectors when
+// the segment is whole and the host-side arrays are 16-byte aligned, so the
+// accesses stay contiguous whether the arrays are device staging buffers or
+// pinned host memory read and written directly over the host link.
+constexpr int kStateBlock = 256;
+__device__ __forceinline__ void aos_in(float* dst, const float* src, int64_t a0, int na, bool vec) {
+  const int tid = threadIdx.x;
+  if (vec && na == kStateBlock) {
+    if (tid < 3 * kStateBlock / 4)
+      reinterpret_cast<float4*>(dst)[tid] = reinterpret_cast<const float4*>(src + 3 * a0)[tid];
+  } else {
+    for (int i = tid; i < 3 * na; i += kStateBlock) dst[i] = src[3 * a0 + i];
+  }
+}
+__device__ __forceinline__ void aos_out(float* dst, const float* src, int64_t a0, int na, bool vec) {
+  const int tid = threadIdx.x;
+  if (vec && na == kStateBlock) {
+    if (tid < 3 * kStateBlock / 4)
+      reinterpret_cast<float4*>(dst + 3 * a0)[tid] = reinterpret_cast<const float4*>(src)[tid];
+  } else {
+    for (int i = tid; i < 3 * na; i += kStateBlock) dst[3 * a0 + i] = src[i];
+  }
+}
+// Upload: positions whose bits change mark their system for a force/list
+// refresh before the next step.
+__global__ void __launch_bounds__(kStateBlock) k_set_state_all(float4* pos, float4* vel, double4_32a* pos64,
+                                                               double4_32a* vel64, const float* xs, const float* vs,
+                                                               const int* atom_sys, SysDev* sys, int64_t n, int vec) {
+  __shared__ __align__(16) float sx[3 * kStateBlock], sv[3 * kStateBlock];
+  const int64_t a0 = (int64_t)blockIdx.x * kStateBlock;
+  const int na = (int)(n - a0 < kStateBlock ? n - a0 : kStateBlock);
+  if (xs) aos_in(sx, xs, a0, na, vec);
+  if (vs) aos_in(sv, vs, a0, na, vec);
+  __syncthreads();
+  const int i = threadIdx.x;
+  if (i >= na) return;
+  const int64_t a = a0 + i;
   const int s = atom_sys[a];
   if (s < 0) return;
   if (xs) {
     const float4 o = pos[a];
-    const float x = xs[3 * a], y = xs[3 * a + 1], z = xs[3 * a + 2];
+    const float x = sx[3 * i], y = sx[3 * i + 1], z = sx[3 * i + 2];
     if (__float_as_uint(x) != __float_as_uint(o.x) || __float_as_uint(y) != __float_as_uint(o.y) ||
         __float_as_uint(z) != __float_as_uint(o.z)) {
       pos[a] = make_float4(x, y, z, o.w);
@@ -641,25 +673,43 @@ __global__ void k_set_state_all(float4* pos, float4* vel, double4_32a* pos64, do
   }
   if (vs) {
     const float4 o = vel[a];
-    vel[a] = make_float4(vs[3 * a], vs[3 * a + 1], vs[3 * a + 2], o.w);
-    if (vel64) vel64[a] = make_double4_32a(vs[3 * a], vs[3 * a + 1], vs[3 * a + 2], vel64[a].w);
+    const float x = sv[3 * i], y = sv[3 * i + 1], z = sv[3 * i + 2];
+    vel[a] = make_float4(x, y, z, o.w);
+    if (vel64) vel64[a] = make_double4_32a(x, y, z, vel64[a].w);
   }
 }
-__global__ void k_get_state_all(const float4* pos, const float4* vel, float* xs, float* vs, int64_t n) {
-  const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (a >= n) return;
-  const float4 p = pos[a], v = vel[a];
-  if (xs) {
-    xs[3 * a] = p.x;
-    xs[3 * a + 1] = p.y;
-    xs[3 * a + 2] = p.z;
+__global__ void __launch_bounds__(kStateBlock) k_get_state_all(const float4* pos, const float4* vel, float* xs,
+                                                               float* vs, int64_t n, int vec) {
+  __shared__ __align__(16) float sx[3 * kStateBlock], sv[3 * kStateBlock];
+  const int64_t a0 = (int64_t)blockIdx.x * kStateBlock;
+  const int na = (int)(n - a0 < kStateBlock ? n - a0 : kStateBlock);
+  const int i = threadIdx.x;
+  if (i < na) {
+    const float4 p = pos[a0 + i], v = vel[a0 + i];
+    sx[3 * i] = p.x;
+    sx[3 * i + 1] = p.y;
+    sx[3 * i + 2] = p.z;
+    sv[3 * i] = v.x;
+    sv[3 * i + 1] = v.y;
+    sv[3 * i + 2] = v.z;
   }
-  if (vs) {
-    vs[3 * a] = v.x;
-    vs[3 * a + 1] = v.y;
-    vs[3 * a + 2] = v.z;
-  }
+  __syncthreads();
+  if (xs) aos_out(xs, sx, a0, na, vec);
+  if (vs) aos_out(vs, sv, a0, na, vec);
 }
+// A host array the kernels may address directly: pinned (page-locked) host
+// memory with a device mapping.  Anything else goes through a staging copy.
+const float* mapped_host(const void* p) {
+  if (!p) return nullptr;
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();  // unregistered pageable memory: not an error, just not mapped
+    return nullptr;
+  }
+  if (at.type != cudaMemoryTypeHost || !at.devicePointer) return nullptr;
+  return static_cast<const float*>(at.devicePointer);
+}
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 __global__ void k_fill_int(int* p, int v, int64_t n) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) p[i] = v;
@@ -1767,16 +1817,25 @@ int64_t prismq_batch_atom_offset(const prismq_batch* b, int32_t slot) {
   return b->slots[slot].atom_b;
 }
 
+// Host arrays in pinned memory are read (written) by the transfer kernel
+// directly; pageable ones go through the device staging buffers.
 prismq_status prismq_batch_set_state_all(prismq_batch* b, const float* xyz, const float* vxyz) {
   if (!b) return fail(PRISMQ_E_INVALID, "batch is NULL");
   const int64_t n = b->atom_span;
   if (n == 0) return PRISMQ_OK;
-  if (xyz) PQ_CK(cudaMemcpyAsync(b->d_stage, xyz, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, b->st));
-  if (vxyz) PQ_CK(cudaMemcpyAsync(b->d_stage2, vxyz, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, b->st));
-  k_set_state_all<<<(unsigned)((n + 255) / 256), 256, 0, b->st>>>(b->A.pos, b->A.vel, b->A.pos64, b->A.vel64,
-                                                                   xyz ? b->d_stage : nullptr,
-                                                                   vxyz ? b->d_stage2 : nullptr, b->A.atom_sys,
-                                                                   b->A.sys, n);
+  const float* xs = mapped_host(xyz);
+  const float* vs = mapped_host(vxyz);
+  if (xyz && !xs) {
+    PQ_CK(cudaMemcpyAsync(b->d_stage, xyz, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, b->st));
+    xs = b->d_stage;
+  }
+  if (vxyz && !vs) {
+    PQ_CK(cudaMemcpyAsync(b->d_stage2, vxyz, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, b->st));
+    vs = b->d_stage2;
+  }
+  const int vec = (!xs || aligned16(xs)) && (!vs || aligned16(vs));
+  k_set_state_all<<<(unsigned)((n + kStateBlock - 1) / kStateBlock), kStateBlock, 0, b->st>>>(
+      b->A.pos, b->A.vel, b->A.pos64, b->A.vel64, xs, vs, b->A.atom_sys, b->A.sys, n, vec);
   g_launches += 1;
   PQ_CK(cudaGetLastError());
   if (xyz) return b->prime_flagged();
@@ -1787,12 +1846,18 @@ prismq_status prismq_batch_get_state_all(prismq_batch* b, float* xyz, float* vxy
   if (!b) return fail(PRISMQ_E_INVALID, "batch is NULL");
   const int64_t n = b->atom_span;
   if (n == 0) return PRISMQ_OK;
-  k_get_state_all<<<(unsigned)((n + 255) / 256), 256, 0, b->st>>>(b->A.pos, b->A.vel, xyz ? b->d_stage : nullptr,
-                                                                   vxyz ? b->d_stage2 : nullptr, n);
+  float* xd = const_cast<float*>(mapped_host(xyz));
+  float* vd = const_cast<float*>(mapped_host(vxyz));
+  const bool stage_x = xyz && !xd, stage_v = vxyz && !vd;
+  if (stage_x) xd = b->d_stage;
+  if (stage_v) vd = b->d_stage2;
+  const int vec = (!xd || aligned16(xd)) && (!vd || aligned16(vd));
+  k_get_state_all<<<(unsigned)((n + kStateBlock - 1) / kStateBlock), kStateBlock, 0, b->st>>>(b->A.pos, b->A.vel,
+                                                                                            xd, vd, n, vec);
   g_launches += 1;
   PQ_CK(cudaGetLastError());
-  if (xyz) PQ_CK(cudaMemcpyAsync(xyz, b->d_stage, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, b->st));
-  if (vxyz) PQ_CK(cudaMemcpyAsync(vxyz, b->d_stage2, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, b->st));
+  if (stage_x) PQ_CK(cudaMemcpyAsync(xyz, b->d_stage, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, b->st));
+  if (stage_v) PQ_CK(cudaMemcpyAsync(vxyz, b->d_stage2, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, b->st));
   PQ_CK(cudaStreamSynchronize(b->st));
   return PRISMQ_OK;
 }

@@ -1,0 +1,96 @@
+"""Whole-arena state transfer (prismq_batch_set_state_all / get_state_all).
+
+Pinned host arrays are read and written by the transfer kernel directly over
+the host link; pageable arrays go through a device staging copy.  Bar: every
+form gives the per-system states bit for bit, including an arena span whose
+last 256-atom block is partial and pinned arrays that are not 16-byte aligned
+(the kernel then moves single words instead of 16-byte vectors), and a
+whole-arena upload continues exactly as the same upload per system.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _pinned(n, offset_floats=0):
+    torch = pytest.importorskip("torch")
+    t = torch.empty(n + offset_floats, dtype=torch.float32, pin_memory=True)
+    return t, t.numpy()[offset_floats:]  # the tensor keeps the pinned block alive
+
+
+def _batch(gpu, topos):
+    b = gpu.Batch(max_atoms=4096, max_systems=4)
+    slots = [b.add_system(t, gpu.Params(stream=k)) for k, t in enumerate(topos)]
+    b.step(12)
+    return b, slots
+
+
+@pytest.fixture(scope="module")
+def topos(gpu):
+    return [gpu.Topology.polyala(1, n, seed=50 + n) for n in (7, 45, 130)]
+
+
+def _views(b, s, n, x, v):
+    o = b.atom_offset(s)
+    return x[3 * o:3 * (o + n)].reshape(-1, 3), v[3 * o:3 * (o + n)].reshape(-1, 3)
+
+
+@pytest.mark.parametrize("form", ["pageable", "pinned", "pinned_misaligned"])
+def test_get_state_all_matches_each_system(gpu, topos, form):
+    b, slots = _batch(gpu, topos)
+    span = b.atom_span()
+    assert span % 256 != 0  # the last transfer block is partial
+    keep = []
+    if form == "pageable":
+        x, v = b.get_state_all()
+    else:
+        off = 1 if form == "pinned_misaligned" else 0
+        tx, x = _pinned(3 * span, off)
+        tv, v = _pinned(3 * span, off)
+        keep += [tx, tv]
+        x[:] = np.nan
+        v[:] = np.nan
+        b.get_state_all(x, v)
+    for s, t in zip(slots, topos):
+        want = b.get_state(s)
+        got = _views(b, s, t.n_atoms, x, v)
+        assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1])
+    b.close()
+
+
+@pytest.mark.parametrize("form", ["pageable", "pinned", "pinned_misaligned"])
+def test_set_state_all_equals_per_system_upload(gpu, topos, form):
+    a, slots = _batch(gpu, topos)
+    ref, rslots = _batch(gpu, topos)
+    span = a.atom_span()
+    x, v = a.get_state_all()
+    x2 = x.copy()
+    v2 = (v * np.float32(0.5)).astype(np.float32)
+    o = a.atom_offset(slots[1])
+    x2[3 * o:3 * o + 3] += np.float32(0.01)  # one moved atom: that system refreshes its list and forces
+    keep = []
+    if form != "pageable":
+        off = 1 if form == "pinned_misaligned" else 0
+        tx, px = _pinned(3 * span, off)
+        tv, pv = _pinned(3 * span, off)
+        keep += [tx, tv]
+        px[:] = x2
+        pv[:] = v2
+        x2, v2 = px, pv
+    a.set_state_all(x2, v2)
+    # per system: velocities everywhere, positions only where bits changed
+    # (the whole-arena upload refreshes only the systems whose positions moved)
+    for k, (s, t) in enumerate(zip(rslots, topos)):
+        xs, vs = _views(a, slots[k], t.n_atoms, np.array(x2), np.array(v2))
+        ref.set_state(s, xs if k == 1 else None, vs)
+    a.step(15)
+    ref.step(15)
+    for s, rs in zip(slots, rslots):
+        xa, va = a.get_state(s)
+        xr, vr = ref.get_state(rs)
+        assert np.array_equal(xa, xr) and np.array_equal(va, vr)
+    a.close()
+    ref.close()
