@@ -913,8 +913,20 @@ void launch_big_cells(const Arena& A, int64_t max_big_atoms, cudaStream_t st) {
     cudaFuncSetAttribute(k_big_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     attr = true;
   }
-  const unsigned atoms_blocks = (unsigned)std::min<int64_t>((max_big_atoms + kBigThreads - 1) / kBigThreads, 4096);
-  const unsigned cell_blocks = (unsigned)std::min<int64_t>((max_big_atoms / 2 + 8) / 8, 4096);  // cells <= atoms / 2
+  // The kernels stride over atoms and cells, and they sit in every step's
+  // graph while a large system is resident, so their grids stay at a few
+  // blocks per SM: on steps without a rebuild every block only reads the
+  // empty work list and leaves.
+  static int cap_blocks = 0;
+  if (!cap_blocks) {
+    int dev = 0, n_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+    cap_blocks = 4 * std::max(n_sm, 1);
+  }
+  const unsigned atoms_blocks =
+      (unsigned)std::min<int64_t>((max_big_atoms + kBigThreads - 1) / kBigThreads, cap_blocks);
+  const unsigned cell_blocks = (unsigned)std::min<int64_t>((max_big_atoms / 2 + 8) / 8, cap_blocks);  // cells <= atoms / 2
   k_big_count<<<atoms_blocks, kBigThreads, 0, st>>>(A);
   k_big_scan<<<1, 1024, 0, st>>>(A);
   k_big_scatter<<<atoms_blocks, kBigThreads, 0, st>>>(A);
