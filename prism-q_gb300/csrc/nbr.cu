@@ -824,8 +824,10 @@ __global__ void __launch_bounds__(kBigThreads) k_big_count(Arena A) {
   }
 }
 
-// One block per large system: the exclusive prefix over its cells, each
-// thread over a contiguous chunk, then a block-wide scan of the chunk sums.
+// One block per large system: the exclusive prefix over its cells in tiles
+// of 1024 cells (one per thread, coalesced), each tile a block-wide scan
+// plus the running total of the tiles before it; the next tile's counts load
+// while the current one is scanned.
 __global__ void __launch_bounds__(1024) k_big_scan(Arena A) {
   __shared__ int wsum[32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -836,40 +838,39 @@ __global__ void __launch_bounds__(1024) k_big_scan(Arena A) {
                                      : Sp->g_dims[0] * Sp->g_dims[1] * Sp->g_dims[2];
     int* start = A.cell_start + Sp->cell_begin;
     int* cursor = start + (Sp->cell_cap + 1);
-    const int chunk = (nc + 1023) / 1024;
-    const int c0 = min(tid * chunk, nc), c1 = min(c0 + chunk, nc);
-    int sum = 0;
     bool ovf = false;
-    for (int c = c0; c < c1; ++c) {
-      const int v = start[c + 1];
+    int carry = 0;
+    int v_next = tid < nc ? start[tid + 1] : 0;
+    for (int base = 0; base < nc; base += 1024) {
+      const int c = base + tid;
+      const int v = v_next;
+      v_next = c + 1024 < nc ? start[c + 1024 + 1] : 0;
       ovf |= v > kCellSortCap;
-      sum += v;
-    }
-    if (ovf) atomicOr(&Sp->status, kStCellOverflow);
-    int x = sum;
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, x, o);
-      if (lane >= o) x += y;
-    }
-    if (lane == 31) wsum[warp] = x;
-    __syncthreads();
-    if (warp == 0) {
-      int w = wsum[lane];
+      int x = v;
       for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(0xffffffffu, w, o);
-        if (lane >= o) w += y;
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
       }
-      wsum[lane] = w;
+      if (lane == 31) wsum[warp] = x;
+      __syncthreads();
+      if (warp == 0) {
+        int w = wsum[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(0xffffffffu, w, o);
+          if (lane >= o) w += y;
+        }
+        wsum[lane] = w;
+      }
+      __syncthreads();
+      const int incl = carry + x + (warp > 0 ? wsum[warp - 1] : 0);
+      if (c < nc) {
+        cursor[c] = incl - v;
+        start[c + 1] = incl;
+      }
+      carry += wsum[31];
+      __syncthreads();  // wsum is rewritten by the next tile
     }
-    __syncthreads();
-    int run = x - sum + (warp > 0 ? wsum[warp - 1] : 0);  // cells before c0
-    for (int c = c0; c < c1; ++c) {
-      const int v = start[c + 1];
-      cursor[c] = run;
-      run += v;
-      start[c + 1] = run;
-    }
-    __syncthreads();
+    if (__syncthreads_or(ovf) && tid == 0) atomicOr(&Sp->status, kStCellOverflow);
   }
 }
 
