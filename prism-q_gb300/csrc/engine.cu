@@ -815,6 +815,10 @@ struct prismq_batch {
     return PRISMQ_OK;
   }
 
+  // The step's row builder keeps a persistent grid once more than two
+  // systems are resident (it then runs beside the other systems' forces).
+  bool build_persistent = false;
+
   void update_spans() {
     const int64_t na = r_atoms.high(), nu = r_units.high();
     int ns = 0;
@@ -834,6 +838,10 @@ struct prismq_batch {
     max_big_atoms = big;
     if (na != atom_span || nu != unit_span || ns != sys_span) graph_dirty = true;
     if ((c32 > 0) != (n_check32 > 0) || (c64 > 0) != (n_check64 > 0)) graph_dirty = true;
+    int resident = 0;
+    for (const SlotRec& R : slots) resident += R.active ? 1 : 0;
+    if ((resident > 2) != build_persistent) graph_dirty = true;
+    build_persistent = resident > 2;
     n_check32 = c32;
     n_check64 = c64;
     atom_span = na;
@@ -893,7 +901,7 @@ struct prismq_batch {
     if (evb) PQ_CK(cudaEventRecordWithFlags(evb[1], st2, cudaEventRecordExternal));
     control(kCtlStep, -1, st);
     if (ev) PQ_CK(cudaEventRecordWithFlags(ev[1], st, cudaEventRecordExternal));
-    launch_nbr_build(A, atom_span, 1, st);
+    launch_nbr_build(A, atom_span, 1, st, build_persistent);
     if (ev) PQ_CK(cudaEventRecordWithFlags(ev[2], st, cudaEventRecordExternal));
     launch_force(A, atom_span, false, st, kSelBranchA, force_variant, group_slots);
     PQ_CK(cudaEventRecord(ev_join, st2));

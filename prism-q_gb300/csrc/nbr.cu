@@ -945,7 +945,15 @@ void launch_control_cells(const Arena& A, int n_sys, int mode, int nbr_override,
   k_control_cells<<<n_sys, kCtlThreads, smem, st>>>(A, mode, nbr_override);
 }
 
-void launch_nbr_build(const Arena& A, int64_t n_atoms_span, int exclude_exceptions, cudaStream_t st) {
+// Grid: with `persistent`, the CTAs that fit on the GPU at once, whose warps
+// stride over the queued groups; otherwise one warp per possible group (CTAs
+// past the queue leave at once).  The persistent grid holds the SMs' registers
+// for the whole build, which suits a builder that runs beside the overlapped
+// force launch of a many-system step; a builder that runs alone (priming, or
+// a step of one or two systems, where a rebuild has nothing to overlap)
+// finishes sooner with every group's warp in flight.
+void launch_nbr_build(const Arena& A, int64_t n_atoms_span, int exclude_exceptions, cudaStream_t st,
+                      bool persistent) {
   if (n_atoms_span <= 0) return;
   static int resident = 0;  // CTAs that fit on the GPU at once
   if (!resident) {
@@ -956,7 +964,8 @@ void launch_nbr_build(const Arena& A, int64_t n_atoms_span, int exclude_exceptio
     resident = std::max(1, n_sm) * std::max(1, per_sm);
   }
   const int64_t groups = (n_atoms_span + 7) / 8;
-  const int grid = (int)std::min<int64_t>(groups, resident);
+  const int64_t per_group = (groups + kNbrThreads / 32 - 1) / (kNbrThreads / 32);
+  const int grid = (int)(persistent ? std::min<int64_t>(groups, resident) : std::min<int64_t>(per_group, 1 << 30));
   k_nbr_build<<<grid, kNbrThreads, 0, st>>>(A, n_atoms_span, exclude_exceptions);
 }
 
