@@ -492,10 +492,10 @@ def run_ours(args, pq, rank, world):
     t_max = max_over_ranks(total_ms.value / 1e3, world)
     total_atoms = sum_over_ranks(float(atoms), world)
     value = total_atoms * args.steps / t_max
-    # per step on the main stream: decision + control, row builder, rebuilt
-    # systems' forces up to the join, noise + integrate; on the second stream
-    # the other systems' forces, overlapping the first three
-    kernels = ["k_decide+k_control_cells", "k_nbr_build", "k_force(rebuilt)+join", "k_noise+k_integrate",
+    # per step on the main stream: decision + control + OU normals, row
+    # builder, rebuilt systems' forces up to the join, integrate; on the second
+    # stream the other systems' forces, overlapping the first three
+    kernels = ["k_decide+k_control_cells+k_noise", "k_nbr_build", "k_force(rebuilt)+join", "k_integrate",
                "k_force(others, overlapped)"]
     phase_avg = {k: statistics.mean(phase_ms[5 * i + p] for i in range(args.steps)) for p, k in enumerate(kernels)}
     # the roofline's kernel: the force kernel over every system, timed alone

@@ -416,10 +416,10 @@ prismq_status prismq_batch_get_state_all(prismq_batch* b, float* xyz, float* vxy
 /* Advance every resident system by n_steps+1 steps, of which n_steps are
  * captured in one CUDA graph and timed on the device: total_ms covers those
  * n_steps; phase_ms (optional, 5*n_steps entries) holds, for step i at
- * [5i..5i+4], the device time on the main stream of (decision + control),
- * row builder, rebuilt systems' forces up to the join, noise + integrate,
- * and then the other systems' force launch on the second stream, which
- * overlaps the first three (events recorded between the launches). */
+ * [5i..5i+4], the device time on the main stream of (decision + control +
+ * OU normals), row builder, rebuilt systems' forces up to the join,
+ * integrate, and then the other systems' force launch on the second stream,
+ * which overlaps the first three (events recorded between the launches). */
 prismq_status prismq_batch_run_timed(prismq_batch* b, int64_t n_steps, float* total_ms, float* phase_ms);
 /* Average device time of the force kernel over every resident system,
  * launched alone n times on the main stream (the roofline's denominator). */

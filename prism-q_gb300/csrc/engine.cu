@@ -856,16 +856,17 @@ struct prismq_batch {
     return PRISMQ_OK;
   }
 
-  // The integrate launch(es) of one step: FP64 batches run one pass; FP32
+  // The integrate launch(es) of one step, after the OU normals (drawn here
+  // unless the step body already drew them): FP64 batches run one pass; FP32
   // batches run one pass per constraint-check precision present.  Returns the
   // number of kernels launched.
-  int integrate(int mode) {
-    launch_noise(A, atom_span, mode, st);
+  int integrate(int mode, bool noise = true) {
+    if (noise) launch_noise(A, atom_span, mode, st);
     if (A.fp64) {
       launch_integrate(A, n_order, mode, st, 0);
-      return 2;
+      return noise ? 2 : 1;
     }
-    int k = 1;
+    int k = noise ? 1 : 0;
     if (n_check32 > 0 || n_check64 == 0) {
       launch_integrate(A, n_order, mode, st, 0);
       ++k;
@@ -891,7 +892,10 @@ struct prismq_batch {
   // ev (optional, 4 events, captured as external records): before k_decide,
   // after the control kernel, after the row builder, after the join.
   // evb (optional, 2): around the branch-B force launch on st2.
-  prismq_status enqueue_step_body(cudaEvent_t* ev = nullptr, cudaEvent_t* evb = nullptr) {
+  // The OU normals of the step's integrate launch (mode) are drawn on st
+  // right after the control kernel: they need only the step's decisions, so
+  // they run beside the forces instead of after the join.
+  prismq_status enqueue_step_body(int mode, cudaEvent_t* ev = nullptr, cudaEvent_t* evb = nullptr) {
     if (ev) PQ_CK(cudaEventRecordWithFlags(ev[0], st, cudaEventRecordExternal));
     launch_decide(A, sys_span, st);
     PQ_CK(cudaEventRecord(ev_fork, st));
@@ -900,6 +904,7 @@ struct prismq_batch {
     launch_force(A, atom_span, false, st2, kSelBranchB, force_variant, group_slots);
     if (evb) PQ_CK(cudaEventRecordWithFlags(evb[1], st2, cudaEventRecordExternal));
     control(kCtlStep, -1, st);
+    launch_noise(A, atom_span, mode, st);
     if (ev) PQ_CK(cudaEventRecordWithFlags(ev[1], st, cudaEventRecordExternal));
     launch_nbr_build(A, atom_span, 1, st, build_persistent);
     if (ev) PQ_CK(cudaEventRecordWithFlags(ev[2], st, cudaEventRecordExternal));
@@ -956,8 +961,9 @@ struct prismq_batch {
     if (part == 0) {
       integrate(kIntPre);
     } else {
-      brc = enqueue_step_body();
-      integrate(part == 1 ? kIntBoth : kIntPost);
+      const int mode = part == 1 ? kIntBoth : kIntPost;
+      brc = enqueue_step_body(mode);
+      integrate(mode, false);
     }
     cudaError_t ce = cudaStreamEndCapture(st, &g);
     if (brc != PRISMQ_OK) return brc;
@@ -1028,8 +1034,8 @@ struct prismq_batch {
   // n steady steps captured in one graph with events between the launches;
   // head and tail phases run outside the timed graph.
   // phase_ms (optional, 5*n entries): for step i the device time of
-  // [decide + control, row builder, branch-A forces up to the join,
-  // noise + integrate] on the main stream, then the branch-B force launch on
+  // [decide + control + OU normals, row builder, branch-A forces up to the
+  // join, integrate] on the main stream, then the branch-B force launch on
   // the second stream (which overlaps the first three).
   prismq_status run_timed(int64_t n, float* total_ms, float* phase_ms) {
     if (n <= 0 || sys_span == 0) return fail(PRISMQ_E_INVALID, "nothing to time");
@@ -1045,8 +1051,8 @@ struct prismq_batch {
     PQ_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     prismq_status brc = PRISMQ_OK;
     for (int64_t i = 0; i < n && brc == PRISMQ_OK; ++i) {
-      brc = enqueue_step_body(&ev[4 * i], &evb[2 * i]);
-      integrate(kIntBoth);
+      brc = enqueue_step_body(kIntBoth, &ev[4 * i], &evb[2 * i]);
+      integrate(kIntBoth, false);
     }
     cudaEventRecordWithFlags(ev[4 * n], st, cudaEventRecordExternal);
     cudaError_t ce = cudaStreamEndCapture(st, &g);
@@ -1071,8 +1077,8 @@ struct prismq_batch {
     cudaGraphExecDestroy(ge);
     for (auto& x : ev) cudaEventDestroy(x);
     for (auto& x : evb) cudaEventDestroy(x);
-    if ((rc = enqueue_step_body()) != PRISMQ_OK) return rc;
-    g_launches += body_launches() + integrate(kIntPost);
+    if ((rc = enqueue_step_body(kIntPost)) != PRISMQ_OK) return rc;
+    g_launches += body_launches() + 1 + integrate(kIntPost, false);
     PQ_CK(cudaGetLastError());
     return check_status();
   }
