@@ -53,6 +53,7 @@ struct Job {
   std::vector<char> resume;  // checkpoint to start from (empty: the topology's own state)
   void* snap = nullptr;      // where the final checkpoint goes
   size_t snap_cap = 0;
+  size_t snap_len = 0;       // bytes written there at retirement
 };
 
 void copy_message(char* dst, size_t cap, const std::string& msg) {
@@ -187,10 +188,8 @@ struct prismq_server {
           js = prismq_batch_get_state(batch, j.slot, j.xout, j.vout);
           if (js != PRISMQ_OK) msg = prismq_last_error();
           if (js == PRISMQ_OK && j.snap) {
-            size_t written = 0;
-            js = prismq_batch_checkpoint_save(batch, j.slot, j.snap, j.snap_cap, &written);
+            js = prismq_batch_checkpoint_save(batch, j.slot, j.snap, j.snap_cap, &j.snap_len);
             if (js != PRISMQ_OK) msg = prismq_last_error();
-            j.snap_cap = js == PRISMQ_OK ? written : 0;
           }
         }
         int64_t steps_done = j.n_steps;
@@ -201,7 +200,7 @@ struct prismq_server {
         }
         prismq_batch_remove_system(batch, j.slot);
         done.push_back(make_result(j, js, steps_done, msg));
-        done.back().snapshot_len = js == PRISMQ_OK && j.snap ? j.snap_cap : 0;
+        done.back().snapshot_len = js == PRISMQ_OK ? j.snap_len : 0;
         (js == PRISMQ_OK ? completed : failed) += 1;
       }
       lk.lock();
