@@ -237,3 +237,17 @@ def test_bad_resume_fails_the_job_alone(gpu, mix, ala40):
         res = _drain(srv, 2)
     assert not res[bad].ok and "corrupted" in res[bad].message and res[bad].steps_done == 0
     assert res[good].ok and np.array_equal(res[good].positions, ref[0])
+
+
+def test_checkpoint_size_for_atoms_is_host_only(pq):
+    """Sizing a served job's snapshot buffer needs no device: a fixed header
+    plus positions, velocities and list-build positions (9 floats per atom)."""
+    L = pq.load()
+    sizes = []
+    for n in (0, 1, 2500, 100_000):
+        out = ctypes.c_size_t()
+        assert L.prismq_checkpoint_size_for_atoms(n, ctypes.byref(out)) == 0
+        sizes.append(out.value)
+    header = sizes[0]
+    assert header > 0 and all(s == header + 36 * n for s, n in zip(sizes, (0, 1, 2500, 100_000)))
+    assert L.prismq_checkpoint_size_for_atoms(-1, ctypes.byref(ctypes.c_size_t())) == 1
