@@ -251,3 +251,40 @@ def test_checkpoint_size_for_atoms_is_host_only(pq):
     header = sizes[0]
     assert header > 0 and all(s == header + 36 * n for s, n in zip(sizes, (0, 1, 2500, 100_000)))
     assert L.prismq_checkpoint_size_for_atoms(-1, ctypes.byref(ctypes.c_size_t())) == 1
+
+
+def _dense_cloud(kind):
+    rng = np.random.default_rng(3)
+    if kind == "rows":  # 8,000 atoms in a 30 Å cube: ≈2,100 partners inside, ≤ 77 atoms per cell
+        return (rng.random((8000, 3)) * 30.0).astype(np.float32)
+    d = rng.normal(size=(1300, 3))  # 1,300 atoms in a 6 Å ball: three cells, > 512 atoms in one
+    d /= np.linalg.norm(d, axis=1)[:, None]
+    return (d * 6.0 * rng.random((1300, 1)) ** (1.0 / 3.0)).astype(np.float32)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind,status", [("rows", 6), ("cells", 5)])
+def test_list_overflow_is_reported_and_isolated(gpu, kind, status):
+    """Clouds dense enough that rows reach the 1024-entry cap
+    (PRISMQ_E_NEIGHBOR_OVERFLOW) or a cell the 512-atom cap
+    (PRISMQ_E_CELL_OVERFLOW): the writes stop at the caps and the system
+    reports the status (no trap).  The system beside it in the same batch is
+    untouched and, once the failed one is removed, continues exactly as it
+    would alone."""
+    dense = gpu.Topology.point_cloud(_dense_cloud(kind))
+    ok = gpu.Topology.polyala(1, 20, seed=5)
+    b = gpu.Batch(max_atoms=12288, max_systems=4)
+    s_ok = b.add_system(ok, gpu.Params(stream=1))
+    s_bad = b.add_system(dense, gpu.Params(stream=2))
+    with pytest.raises(gpu.PrismQError) as e:
+        b.step(5)
+    assert e.value.status == status
+    assert b.status(s_bad) == status
+    assert b.status(s_ok) == 0
+    done = b.timestep(s_ok)
+    b.remove_system(s_bad)
+    b.step(7)
+    x, v = b.get_state(s_ok)
+    b.close()
+    xr, vr = _alone(gpu, ok, gpu.Params(stream=1), done + 7)
+    assert np.array_equal(x, xr) and np.array_equal(v, vr)
