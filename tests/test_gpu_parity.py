@@ -283,3 +283,36 @@ def test_invalid_topology_rejected_on_host(gpu, ala40):
     bad2.bonds["j"][0] = ala40.n_atoms + 5
     with pytest.raises(gpu.PrismQError):
         gpu.NhsAmberFusedEngine(bad2, gpu.Params())
+
+
+def test_tiny_and_ragged_systems(gpu, orc):
+    """Systems of 1, 2 and 3 atoms (partial force groups, warps and cells)
+    step beside a 70-atom chain: a lone atom feels exactly zero force; a pair
+    and a triple match the FP64 oracle; after 30 steps every state is finite
+    and each system equals its solo run."""
+    clouds = [np.array([[1.0, 2.0, 3.0]], np.float32),
+              np.array([[0.0, 0.0, 0.0], [3.6, 0.5, -0.2]], np.float32),
+              np.array([[0.0, 0.0, 0.0], [3.8, 0.0, 0.0], [0.0, 4.1, 0.3]], np.float32)]
+    topos = [gpu.Topology.point_cloud(c) for c in clouds] + [gpu.Topology.polyala(1, 7, seed=2)]
+    for t in topos[:3]:
+        eng = gpu.NhsAmberFusedEngine(t, gpu.Params())
+        _, f, fx = eng.compute_forces()
+        if t.n_atoms == 1:
+            assert not fx.any()
+        else:
+            f64, _ = _oracle(orc, t, gpu.Params()).forces_f64()
+            assert rel_rms(f, f64) <= FORCE_RTOL
+        eng.close()
+    b = gpu.Batch(max_atoms=1024, max_systems=8)
+    slots = [b.add_system(t, gpu.Params(stream=k)) for k, t in enumerate(topos)]
+    b.step(30)
+    for k, (s, t) in enumerate(zip(slots, topos)):
+        x, v = b.get_state(s)
+        assert np.isfinite(x).all() and np.isfinite(v).all()
+        solo = gpu.Batch(max_atoms=t.n_atoms + 64, max_systems=1)
+        ss = solo.add_system(t, gpu.Params(stream=k))
+        solo.step(30)
+        xs, vs = solo.get_state(ss)
+        solo.close()
+        assert np.array_equal(x, xs) and np.array_equal(v, vs)
+    b.close()
