@@ -13,10 +13,10 @@
 //
 // One step on the device, captured once per batch shape in a CUDA graph:
 // the schedule decision (per system) → [control+cells of the rebuilding
-// systems → their neighbour rows → their forces] beside [the forces of the
-// other systems on a second stream] → the OU normals → integrate (post-phases
-// of this step fused with pre-phases of the next).  Systems of 16k+ atoms
-// add four grid-wide cell-sort launches after the control kernel.
+// systems → the OU normals → their neighbour rows → their forces] beside
+// [the forces of the other systems on a second stream] → integrate
+// (post-phases of this step fused with pre-phases of the next).  Systems of
+// 16k+ atoms add four grid-wide cell-sort launches after the control kernel.
 #include <cuda_runtime.h>
 #include <nvtx3/nvToolsExt.h>
 
