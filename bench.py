@@ -512,16 +512,14 @@ def run_ours(args, pq, rank, world):
     hv = torch.empty(3 * span, dtype=torch.float32, pin_memory=True).numpy()
     L = pq.load()
     L.prismq_batch_get_state_all(batch.h, hx.ctypes.data, hv.ctypes.data)
+    # each step: upload x, v from the pinned arrays, one step, read x, v back
+    # into them -- one C-ABI call (prismq_batch_step_host) with one wait
     for _ in range(2):
-        L.prismq_batch_set_state_all(batch.h, hx.ctypes.data, hv.ctypes.data)
-        batch.step(1)
-        L.prismq_batch_get_state_all(batch.h, hx.ctypes.data, hv.ctypes.data)
+        batch.step_host(1, hx, hv, hx, hv)
     barrier(world)
     t0 = time.perf_counter()
     for _ in range(args.e2e_steps):
-        rc = L.prismq_batch_set_state_all(batch.h, hx.ctypes.data, hv.ctypes.data)
-        rc |= L.prismq_batch_step(batch.h, 1)
-        rc |= L.prismq_batch_get_state_all(batch.h, hx.ctypes.data, hv.ctypes.data)
+        rc = L.prismq_batch_step_host(batch.h, 1, hx.ctypes.data, hv.ctypes.data, hx.ctypes.data, hv.ctypes.data)
         if rc:
             raise pq.PrismQError(rc, L.prismq_last_error().decode())
     e2e_t = max_over_ranks(time.perf_counter() - t0, world)

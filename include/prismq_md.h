@@ -413,6 +413,13 @@ int64_t prismq_batch_atom_span(const prismq_batch* b);
 int64_t prismq_batch_atom_offset(const prismq_batch* b, int32_t slot);
 prismq_status prismq_batch_set_state_all(prismq_batch* b, const float* xyz, const float* vxyz);
 prismq_status prismq_batch_get_state_all(prismq_batch* b, float* xyz, float* vxyz);
+/* A host-driven step in one call: set_state_all(xyz_in, vxyz_in), n_steps
+ * steps, get_state_all(xyz_out, vxyz_out), enqueued back to back with one
+ * wait at the end (any array may be NULL; n_steps 0 only transfers).  The
+ * outputs are filled even when a system fails; the return value is then
+ * that failure, as from prismq_batch_step. */
+prismq_status prismq_batch_step_host(prismq_batch* b, int64_t n_steps, const float* xyz_in, const float* vxyz_in,
+                                     float* xyz_out, float* vxyz_out);
 /* Advance every resident system by n_steps+1 steps, of which n_steps are
  * captured in one CUDA graph and timed on the device: total_ms covers those
  * n_steps; phase_ms (optional, 5*n_steps entries) holds, for step i at

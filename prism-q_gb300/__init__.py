@@ -218,6 +218,7 @@ def load() -> ctypes.CDLL:
         "prismq_batch_atom_offset": (i64, [P, ctypes.c_int32]),
         "prismq_batch_set_state_all": (I, [P, P, P]),
         "prismq_batch_get_state_all": (I, [P, P, P]),
+        "prismq_batch_step_host": (I, [P, ctypes.c_int64, P, P, P, P]),
         "prismq_batch_run_timed": (I, [P, i64, P, P]),
         "prismq_batch_time_force": (I, [P, ctypes.c_int32, P]),
         "prismq_batch_counters": (I, [P, ctypes.c_int32, P]),
@@ -756,6 +757,16 @@ class Batch:
             if a is not None and (a.dtype != np.float32 or a.size != n or not a.flags.c_contiguous):
                 raise ValueError(f"state arrays must be contiguous float32 of {n} values")
         _check(load().prismq_batch_set_state_all(self.h, _ptr(xyz), _ptr(vxyz)))
+
+    def step_host(self, n_steps: int, xyz_in, vxyz_in, xyz_out, vxyz_out) -> None:
+        """Upload whole-arena state, step, and read it back in one call (one
+        wait); arrays are float32 [3 * atom_span] or None."""
+        n = 3 * self.atom_span()
+        for a in (xyz_in, vxyz_in, xyz_out, vxyz_out):
+            if a is not None and (a.dtype != np.float32 or a.size != n or not a.flags.c_contiguous):
+                raise ValueError(f"state arrays must be contiguous float32 of {n} values")
+        _check(load().prismq_batch_step_host(self.h, int(n_steps), _ptr(xyz_in), _ptr(vxyz_in), _ptr(xyz_out),
+                                             _ptr(vxyz_out)))
 
     def set_force_variant(self, variant: int) -> int:
         """Pin the force kernel's launch shape (-1: autotune); returns the number of shapes."""

@@ -1155,7 +1155,9 @@ struct prismq_batch {
     return step_segment(n);
   }
 
-  prismq_status step_segment(int64_t n) {
+  // `check` false: the launches are enqueued and the status check is left to
+  // the caller (prismq_batch_step_host reads the status with the state).
+  prismq_status step_segment(int64_t n, bool check = true) {
     prismq_status rc = prime_if_needed();
     if (rc != PRISMQ_OK) return rc;
     rc = ensure_graph();
@@ -1166,7 +1168,13 @@ struct prismq_batch {
     PQ_CK(cudaGraphLaunch(gexec_tail, st));
     g_launches += (int64_t)per_step * n + integrate_passes();  // head: the noise and integrate launches once more
     PQ_CK(cudaGetLastError());
-    return check_status();
+    return check ? check_status() : PRISMQ_OK;
+  }
+
+  bool recording_frames() const {
+    for (int i = 0; i < sys_span; ++i)
+      if (slots[i].active && slots[i].fr_interval > 0) return true;
+    return false;
   }
 };
 
@@ -1856,8 +1864,8 @@ prismq_status prismq_batch_set_state_all(prismq_batch* b, const float* xyz, cons
   return PRISMQ_OK;
 }
 
-prismq_status prismq_batch_get_state_all(prismq_batch* b, float* xyz, float* vxyz) {
-  if (!b) return fail(PRISMQ_E_INVALID, "batch is NULL");
+// Enqueue the whole-arena read-back on the batch stream (no synchronisation).
+static prismq_status enqueue_get_state_all(prismq_batch* b, float* xyz, float* vxyz) {
   const int64_t n = b->atom_span;
   if (n == 0) return PRISMQ_OK;
   float* xd = const_cast<float*>(mapped_host(xyz));
@@ -1872,8 +1880,38 @@ prismq_status prismq_batch_get_state_all(prismq_batch* b, float* xyz, float* vxy
   PQ_CK(cudaGetLastError());
   if (stage_x) PQ_CK(cudaMemcpyAsync(xyz, b->d_stage, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, b->st));
   if (stage_v) PQ_CK(cudaMemcpyAsync(vxyz, b->d_stage2, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, b->st));
+  return PRISMQ_OK;
+}
+
+prismq_status prismq_batch_get_state_all(prismq_batch* b, float* xyz, float* vxyz) {
+  if (!b) return fail(PRISMQ_E_INVALID, "batch is NULL");
+  prismq_status rc = enqueue_get_state_all(b, xyz, vxyz);
+  if (rc != PRISMQ_OK) return rc;
   PQ_CK(cudaStreamSynchronize(b->st));
   return PRISMQ_OK;
+}
+
+// Upload, n steps and read-back in one call: the three are enqueued back to
+// back and the host waits once, for the state and the status words together.
+prismq_status prismq_batch_step_host(prismq_batch* b, int64_t n_steps, const float* xyz_in, const float* vxyz_in,
+                                     float* xyz_out, float* vxyz_out) {
+  if (!b) return fail(PRISMQ_E_INVALID, "batch is NULL");
+  prismq_status rc = prismq_batch_set_state_all(b, xyz_in, vxyz_in);
+  if (rc != PRISMQ_OK) return rc;
+  prismq_status step_rc = PRISMQ_OK;
+  bool status_pending = false;  // the steps' status words are read after the state
+  if (n_steps > 0 && b->sys_span > 0) {
+    if (b->recording_frames()) {
+      step_rc = b->step(n_steps);  // frame segments synchronise on their own
+    } else {
+      if ((rc = b->step_segment(n_steps, false)) != PRISMQ_OK) return rc;
+      status_pending = true;
+    }
+  }
+  if ((rc = enqueue_get_state_all(b, xyz_out, vxyz_out)) != PRISMQ_OK) return rc;
+  if (status_pending) return b->check_status();  // its read-back waits for the state too
+  PQ_CK(cudaStreamSynchronize(b->st));
+  return step_rc;
 }
 
 int64_t prismq_batch_resident_atoms(const prismq_batch* b) {

@@ -94,3 +94,35 @@ def test_set_state_all_equals_per_system_upload(gpu, topos, form):
         assert np.array_equal(xa, xr) and np.array_equal(va, vr)
     a.close()
     ref.close()
+
+
+@pytest.mark.parametrize("form", ["pageable", "pinned"])
+def test_step_host_equals_upload_step_download(gpu, topos, form):
+    """prismq_batch_step_host (upload, steps, read-back, one wait) gives the
+    same bits as the three calls, in place (the same arrays in and out) or
+    not, and with n_steps 0 it only transfers."""
+    a, _ = _batch(gpu, topos)
+    b, _ = _batch(gpu, topos)
+    span = a.atom_span()
+    x, v = a.get_state_all()
+    v = (v * np.float32(0.9)).astype(np.float32)
+    keep = []
+    if form == "pinned":
+        tx, px = _pinned(3 * span)
+        tv, pv = _pinned(3 * span)
+        keep += [tx, tv]
+        px[:] = x
+        pv[:] = v
+        x, v = px, pv
+    xr, vr = x.copy(), v.copy()
+    for _ in range(3):
+        a.step_host(4, x, v, x, v)  # in place
+        b.set_state_all(xr, vr)
+        b.step(4)
+        b.get_state_all(xr, vr)
+        assert np.array_equal(x, xr) and np.array_equal(v, vr)
+    xo, vo = np.empty_like(xr), np.empty_like(vr)
+    a.step_host(0, None, None, xo, vo)
+    assert np.array_equal(xo, xr) and np.array_equal(vo, vr)
+    a.close()
+    b.close()
