@@ -14,14 +14,18 @@
 //                    that rows come out in a deterministic order without a
 //                    per-row sort.  It then queues the 8-atom groups of every
 //                    rebuilding system on a device work list.
-//   k_nbr_build      persistent (all resident CTAs): warps walk the queued
-//                    atoms round-robin; one warp per atom scans the stencil row
-//                    by row (the x-run of cells in one (y, z) row is one
-//                    contiguous run of sorted atoms, trimmed per atom to the
-//                    sphere of radius r_list, so warps stay full), applies the
-//                    exclusion window bitmask and ballot-compacts the kept
-//                    atoms straight into the tiled layout the force kernel
-//                    reads.  Steps without rebuilds cost one empty pass.
+//   k_nbr_build      one warp per queued 8-atom group (a persistent grid of
+//                    the resident CTAs when it runs beside the forces of a
+//                    many-system step, every group's warp at once when it
+//                    runs alone).  The warp lists the cell-row runs of the
+//                    union of its atoms' stencils (the x-run of cells in one
+//                    (y, z) row is one contiguous run of sorted atoms), streams
+//                    their candidates in full 32-lane chunks, tests each
+//                    against the eight atoms, applies the exclusion window
+//                    bitmask and ballot-compacts the kept atoms straight into
+//                    the tiled layout the force kernel reads.  REF27 rows are
+//                    built atom by atom with the reference's stencil.  Steps
+//                    without rebuilds cost one empty pass.
 // Complete mode uses cells at least r_list/2 wide with a ±2 stencil (every
 // pair within r_list is found); REF27 mode reproduces the reference pair set.
 #include <algorithm>
