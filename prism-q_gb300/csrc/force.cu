@@ -12,8 +12,9 @@
 //
 // GB300 form: the same ownership (no force atomics), but
 //   * positions+charges stream as float4 and LJ as float2 (σ/2, √ε);
-//   * neighbour rows are interleaved by 8-atom group so a warp's index loads
-//     are one 128-byte line per k, and exception pairs are already excluded
+//   * neighbour rows are interleaved by 8-atom group so that a lane reads its
+//     next four row indices as one int4 and a warp's index loads are one
+//     contiguous 512-byte block, and exception pairs are already excluded
 //     from the rows (no per-neighbour 1-4 scan);
 //   * partial sums are FP32 over at most 32 pairs and then accumulated in
 //     int64 fixed point at 2^-32 kcal/mol/Å, so the force of an atom is a
