@@ -161,6 +161,24 @@ typedef struct prismq_topology_buf prismq_topology_buf;
 prismq_status prismq_polyala_build(int32_t n_chains, int32_t n_residues, uint64_t seed,
                                    float density, float box_edge,
                                    prismq_topology_buf** out);
+/* The same chains collapsed into compact systems, the synthetic inputs of the
+ * benchmark configurations (a random-walk backbone collapsed into a globule;
+ * chains packed without overlap in a cube).  The chains are grown at
+ * 0.02 atoms/Å^3 and then squeezed by a deterministic relaxation: bond and
+ * angle restraints from the topology, a contact distance of
+ * max(0.8 (Rmin_i/2 + Rmin_j/2), 2 Å) between atoms more than three bonds
+ * apart, and a region that shrinks to its target:
+ *   box_edge <= 0: one sphere per chain holding it at `density` atoms/Å^3
+ *                  (<= 0 selects 0.0746: 2,500 atoms in a 40 Å globule);
+ *   box_edge  > 0: one cube of edge box_edge holding every chain.
+ * Hydrogens end on their constraint lengths.  stats (may be NULL) receives:
+ * relaxation iterations, the largest remaining contact overlap (Å), the
+ * largest distance of an atom outside its region (Å), and the closest pair
+ * of atoms more than three bonds apart (Å).  Deterministic for a given seed,
+ * with identical bits on x86-64 and aarch64. */
+prismq_status prismq_polyala_build_compact(int32_t n_chains, int32_t n_residues, uint64_t seed,
+                                           float density, float box_edge, double stats[4],
+                                           prismq_topology_buf** out);
 /* View the arrays of a built topology; valid until prismq_topology_free. */
 prismq_status prismq_topology_view(const prismq_topology_buf* buf, prismq_topology* out);
 void prismq_topology_free(prismq_topology_buf* buf);

@@ -1633,6 +1633,22 @@ prismq_status prismq_polyala_build(int32_t n_chains, int32_t n_residues, uint64_
   return PRISMQ_OK;
 }
 
+prismq_status prismq_polyala_build_compact(int32_t n_chains, int32_t n_residues, uint64_t seed, float density,
+                                           float box_edge, double* stats, prismq_topology_buf** out) {
+  if (!out) return fail(PRISMQ_E_INVALID, "out is NULL");
+  auto* b = new prismq_topology_buf();
+  std::string err;
+  double st[4] = {0.0, 0.0, 0.0, 0.0};
+  if (!polyala_build(n_chains, n_residues, seed, density, box_edge, &b->topo, &err, 1, st)) {
+    delete b;
+    return fail(PRISMQ_E_INVALID, err);
+  }
+  if (stats)
+    for (int k = 0; k < 4; ++k) stats[k] = st[k];
+  *out = b;
+  return PRISMQ_OK;
+}
+
 prismq_status prismq_topology_view(const prismq_topology_buf* buf, prismq_topology* out) {
   if (!buf || !out) return fail(PRISMQ_E_INVALID, "NULL argument");
   buf->topo.view(out);

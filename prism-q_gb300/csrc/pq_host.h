@@ -44,8 +44,13 @@ struct HostTopology {
   }
 };
 
+// Seeded poly-alanine-like chains (topology.cpp).  compact = 0: grown at
+// `density` (atoms/Å^3) in their regions; compact = 1: grown sparse and then
+// squeezed to `density` (sphere systems) or into the cube of edge box_edge.
+// squeeze_stats (may be NULL, compact only): iterations, max contact overlap
+// (Å), max wall violation (Å), closest pair more than three bonds apart (Å).
 bool polyala_build(int n_chains, int n_res, uint64_t seed, double density, double box_edge,
-                   HostTopology* T, std::string* err);
+                   HostTopology* T, std::string* err, int compact = 0, double* squeeze_stats = nullptr);
 
 // Engine hooks for the job server (defined in engine.cu).  A job's topology is
 // validated and lowered once on the submitting thread (prepare_system); the

@@ -6,7 +6,9 @@
 // exceptions and hydrogen clusters.  Force-field numbers are the archived
 // ff14SB tables (.archive/crates/prism-physics/src/amber_ff14sb.rs:367-741,
 // :919-970).  Geometry is grown residue by residue with ideal internal
-// coordinates inside a confining sphere or box, rejecting clashes.
+// coordinates inside a confining sphere or box, rejecting clashes; compact
+// systems are grown sparse and then squeezed into their target region
+// (squeeze(), below).
 //
 // All floating-point work here uses IEEE-exact operations and project-written
 // series for sin/cos/log, so the same seed yields the same bits on x86-64 and
@@ -262,6 +264,11 @@ struct Region {
   V3 center;
   double radius;
   V3 lo, hi;
+  // Optional pull point of the growth (a chain's slot inside a shared box):
+  // the first residue starts near it and candidates are weighted toward it.
+  bool has_pull = false;
+  V3 pull;
+  double pull_scale = 0.0;
   bool inside(V3 p, double margin) const {
     if (sphere) {
       const V3 d = p - center;
@@ -406,6 +413,10 @@ static bool grow_chain(Builder& B, int chain, int n_res, int res_base, const Reg
     centre = 0.5 * (reg.lo + reg.hi);
     const V3 h = 0.5 * (reg.hi - reg.lo);
     scale = std::max(h.x, std::max(h.y, h.z));
+  }
+  if (reg.has_pull) {
+    centre = reg.pull;
+    scale = reg.pull_scale;
   }
   long long attempts = 0;
   const long long max_attempts = 400LL * n_res + 2000;
@@ -652,14 +663,342 @@ static void assemble(const Builder& B, int n_chains, int n_res, HostTopology* T)
   for (int a = 0; a < n; ++a) T->masses[a] = (float)mass[a];
 }
 
+// --------------------------------------------------------------------------
+// Compaction: the grown chains are squeezed into their target region by a
+// FIRE relaxation (Bitzek et al., Phys. Rev. Lett. 97, 170201 (2006)) of a
+// restraint energy while a wall shrinks from the grown extent to the target:
+//   bonds   k_b (r - r0)^2                 (r0 from the topology)
+//   angles  k_a (cos θ - cos θ0)^2         (θ0 from the topology)
+//   contact k_r (d_ij - r)^2 for r < d_ij  (every pair more than three bonds
+//           apart; d_ij = max(0.8 (Rmin_i/2 + Rmin_j/2), 2 Å) from the ff14SB
+//           LJ radii)
+//   wall    k_w s^2, s the distance of an atom outside the region.
+// Arithmetic is +, -, *, / and sqrt in a fixed order (sums over atoms run in
+// index order), so the result has the same bits on every IEEE machine.  After
+// the relaxation each hydrogen is moved along its bond to the constraint
+// length, so SHAKE starts from satisfied constraints.
+// --------------------------------------------------------------------------
+struct SqueezeRegion {
+  bool sphere = true;
+  std::vector<V3> centre;  // per chain (sphere systems)
+  double r_start = 0.0, r_target = 0.0;
+  V3 lo0, hi0, lo1, hi1;  // box: start and target
+};
+
+struct SqueezeReport {
+  int iterations = 0;
+  double max_overlap = 0.0;   // max (d_ij - r) over contact pairs
+  double max_outside = 0.0;   // max wall violation (Å)
+  double min_nonbonded = 0.0; // closest pair more than three bonds apart (Å)
+};
+
+static double contact_radius(int type) { return kLJ[type].rmin_half; }
+
+static void squeeze(HostTopology* T, const std::vector<int>& types, int atoms_per_chain, const SqueezeRegion& reg,
+                    SqueezeReport* rep) {
+  const int n = T->n_atoms;
+  const size_t n3 = 3 * (size_t)n;
+  std::vector<double> x(n3), v(n3, 0.0), f(n3), xl(n3);
+  for (size_t k = 0; k < n3; ++k) x[k] = (double)T->positions[k];
+  const double kb = 100.0, ka = 50.0, kr = 50.0, kw = 100.0;
+  std::vector<double> cos0(T->angles.size());
+  for (size_t t = 0; t < T->angles.size(); ++t) {
+    double s, c;
+    det::sincos((double)T->angles[t].theta0, &s, &c);
+    cos0[t] = c;
+  }
+  std::vector<double> rad(n);
+  double rad_max = 0.0;
+  for (int a = 0; a < n; ++a) {
+    rad[a] = contact_radius(types[a]);
+    rad_max = std::max(rad_max, rad[a]);
+  }
+  const double dmax = std::max(2.0, 1.6 * rad_max);
+  const double skin = 1.2, rl = dmax + skin, rl2 = rl * rl;
+  const int32_t* eo = T->exclusion_offsets.data();
+  const int32_t* ex = T->exclusions.data();
+  auto excluded = [&](int i, int j) { return std::binary_search(ex + eo[i], ex + eo[i + 1], j); };
+  // Contact pairs within rl (i < j) in the order of i, then of the cell walk
+  // (cells hold atoms in index order), which is fixed by the positions.
+  std::vector<int> pi_, pj_;
+  std::vector<double> pd;
+  std::vector<int> head, order, cell;
+  double shrink_since_build = 1.0;  // product of the scale factors applied since the last build
+  auto build_pairs = [&]() {
+    pi_.clear();
+    pj_.clear();
+    pd.clear();
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int a = 0; a < n; ++a)
+      for (int d = 0; d < 3; ++d) {
+        lo[d] = std::min(lo[d], x[3 * a + d]);
+        hi[d] = std::max(hi[d], x[3 * a + d]);
+      }
+    long long dims[3];
+    double inv[3];
+    for (int d = 0; d < 3; ++d) {
+      dims[d] = std::max(1LL, (long long)((hi[d] - lo[d]) / rl));
+      inv[d] = (double)dims[d] / (hi[d] - lo[d] + 1e-9);
+    }
+    const long long ncell = dims[0] * dims[1] * dims[2];
+    head.assign(ncell + 1, 0);
+    order.resize(n);
+    cell.resize(n);
+    for (int a = 0; a < n; ++a) {
+      long long c3[3];
+      for (int d = 0; d < 3; ++d) {
+        const long long c = (long long)((x[3 * a + d] - lo[d]) * inv[d]);
+        c3[d] = std::min(std::max(c, 0LL), dims[d] - 1);
+      }
+      cell[a] = (int)(c3[0] + dims[0] * (c3[1] + dims[1] * c3[2]));
+      head[cell[a] + 1] += 1;
+    }
+    for (long long c = 0; c < ncell; ++c) head[c + 1] += head[c];
+    {
+      std::vector<int> cur(head.begin(), head.end() - 1);
+      for (int a = 0; a < n; ++a) order[cur[cell[a]]++] = a;
+    }
+    for (int a = 0; a < n; ++a) {
+      const long long c = cell[a];
+      const long long cx = c % dims[0], cy = (c / dims[0]) % dims[1], cz = c / (dims[0] * dims[1]);
+      const double xa = x[3 * a], ya = x[3 * a + 1], za = x[3 * a + 2];
+      for (long long dz = -1; dz <= 1; ++dz)
+        for (long long dy = -1; dy <= 1; ++dy)
+          for (long long dx = -1; dx <= 1; ++dx) {
+            const long long X = cx + dx, Y = cy + dy, Z = cz + dz;
+            if (X < 0 || Y < 0 || Z < 0 || X >= dims[0] || Y >= dims[1] || Z >= dims[2]) continue;
+            const long long o = X + dims[0] * (Y + dims[1] * Z);
+            for (int k = head[o]; k < head[o + 1]; ++k) {
+              const int b = order[k];
+              if (b <= a) continue;
+              const double ddx = x[3 * b] - xa, ddy = x[3 * b + 1] - ya, ddz = x[3 * b + 2] - za;
+              if (ddx * ddx + ddy * ddy + ddz * ddz > rl2) continue;
+              if (excluded(a, b)) continue;
+              pi_.push_back(a);
+              pj_.push_back(b);
+              pd.push_back(std::max(0.8 * (rad[a] + rad[b]), 2.0));
+            }
+          }
+    }
+    xl = x;
+    shrink_since_build = 1.0;
+  };
+  double max_overlap = 0.0, max_outside = 0.0;
+  auto forces = [&](bool wall) {
+    std::fill(f.begin(), f.end(), 0.0);
+    for (const prismq_bond& b : T->bonds) {
+      const int i = b.i, j = b.j;
+      const double dx = x[3 * j] - x[3 * i], dy = x[3 * j + 1] - x[3 * i + 1], dz = x[3 * j + 2] - x[3 * i + 2];
+      const double r = std::sqrt(dx * dx + dy * dy + dz * dz);
+      if (r < 1e-9) continue;
+      const double s = 2.0 * kb * (r - (double)b.r0) / r;  // pulls i toward j when stretched
+      f[3 * i] += s * dx; f[3 * i + 1] += s * dy; f[3 * i + 2] += s * dz;
+      f[3 * j] -= s * dx; f[3 * j + 1] -= s * dy; f[3 * j + 2] -= s * dz;
+    }
+    for (size_t t = 0; t < T->angles.size(); ++t) {
+      const prismq_angle& g = T->angles[t];
+      const int i = g.i, j = g.j, k = g.k;
+      const double ux = x[3 * i] - x[3 * j], uy = x[3 * i + 1] - x[3 * j + 1], uz = x[3 * i + 2] - x[3 * j + 2];
+      const double wx = x[3 * k] - x[3 * j], wy = x[3 * k + 1] - x[3 * j + 1], wz = x[3 * k + 2] - x[3 * j + 2];
+      const double uu = ux * ux + uy * uy + uz * uz, ww = wx * wx + wy * wy + wz * wz;
+      if (uu < 1e-18 || ww < 1e-18) continue;
+      const double inv = 1.0 / (std::sqrt(uu) * std::sqrt(ww));
+      const double c = (ux * wx + uy * wy + uz * wz) * inv;
+      const double g2 = -2.0 * ka * (c - cos0[t]);  // -dE/dc
+      const double ai = c / uu, ak = c / ww;
+      const double fix = g2 * (wx * inv - ai * ux), fiy = g2 * (wy * inv - ai * uy), fiz = g2 * (wz * inv - ai * uz);
+      const double fkx = g2 * (ux * inv - ak * wx), fky = g2 * (uy * inv - ak * wy), fkz = g2 * (uz * inv - ak * wz);
+      f[3 * i] += fix; f[3 * i + 1] += fiy; f[3 * i + 2] += fiz;
+      f[3 * k] += fkx; f[3 * k + 1] += fky; f[3 * k + 2] += fkz;
+      f[3 * j] -= fix + fkx; f[3 * j + 1] -= fiy + fky; f[3 * j + 2] -= fiz + fkz;
+    }
+    max_overlap = 0.0;
+    for (size_t p = 0; p < pi_.size(); ++p) {
+      const int i = pi_[p], j = pj_[p];
+      const double dx = x[3 * j] - x[3 * i], dy = x[3 * j + 1] - x[3 * i + 1], dz = x[3 * j + 2] - x[3 * i + 2];
+      const double r2 = dx * dx + dy * dy + dz * dz, d = pd[p];
+      if (r2 >= d * d) continue;
+      const double r = std::sqrt(r2);
+      if (r < 1e-9) continue;
+      max_overlap = std::max(max_overlap, d - r);
+      const double s = 2.0 * kr * (d - r) / r;  // pushes i away from j
+      f[3 * i] -= s * dx; f[3 * i + 1] -= s * dy; f[3 * i + 2] -= s * dz;
+      f[3 * j] += s * dx; f[3 * j + 1] += s * dy; f[3 * j + 2] += s * dz;
+    }
+    max_outside = 0.0;
+    if (!wall) return;
+    if (reg.sphere) {
+      const double R = reg.r_target;
+      for (int a = 0; a < n; ++a) {
+        const V3 c = reg.centre[a / atoms_per_chain];
+        const double dx = x[3 * a] - c.x, dy = x[3 * a + 1] - c.y, dz = x[3 * a + 2] - c.z;
+        const double r = std::sqrt(dx * dx + dy * dy + dz * dz);
+        if (r <= R) continue;
+        const double s = r - R;
+        max_outside = std::max(max_outside, s);
+        const double g = -2.0 * kw * s / r;
+        f[3 * a] += g * dx; f[3 * a + 1] += g * dy; f[3 * a + 2] += g * dz;
+      }
+    } else {
+      const double lo[3] = {reg.lo1.x, reg.lo1.y, reg.lo1.z}, hi[3] = {reg.hi1.x, reg.hi1.y, reg.hi1.z};
+      for (int a = 0; a < n; ++a)
+        for (int d = 0; d < 3; ++d) {
+          const double p = x[3 * a + d];
+          if (p > hi[d]) {
+            max_outside = std::max(max_outside, p - hi[d]);
+            f[3 * a + d] -= 2.0 * kw * (p - hi[d]);
+          } else if (p < lo[d]) {
+            max_outside = std::max(max_outside, lo[d] - p);
+            f[3 * a + d] += 2.0 * kw * (lo[d] - p);
+          }
+        }
+    }
+  };
+  // One compression step: every atom moves toward its region's centre by the
+  // factor s (the list-build positions too, so the displacement test below
+  // sees only the relaxation's own motion).
+  auto scale_all = [&](double s) {
+    for (int a = 0; a < n; ++a) {
+      V3 c;
+      if (reg.sphere) {
+        c = reg.centre[a / atoms_per_chain];
+      } else {
+        c = 0.5 * (reg.lo0 + reg.hi0);
+      }
+      const double cc[3] = {c.x, c.y, c.z};
+      for (int d = 0; d < 3; ++d) {
+        x[3 * a + d] = cc[d] + s * (x[3 * a + d] - cc[d]);
+        xl[3 * a + d] = cc[d] + s * (xl[3 * a + d] - cc[d]);
+      }
+    }
+    shrink_since_build *= s;
+  };
+  // FIRE parameters (Bitzek et al. 2006), unit masses
+  const double dt_max = 0.08, f_inc = 1.1, f_dec = 0.5, a_start = 0.1, f_a = 0.99, max_step = 0.1;
+  const int n_min = 5;
+  double dt = 0.02, alpha = a_start;
+  int n_pos = 0;
+  auto fire_step = [&](bool wall) {
+    forces(wall);
+    double P = 0.0, vv = 0.0, ff = 0.0;
+    for (size_t k = 0; k < n3; ++k) {
+      P += f[k] * v[k];
+      vv += v[k] * v[k];
+      ff += f[k] * f[k];
+    }
+    if (P > 0.0) {
+      const double sc = ff > 0.0 ? alpha * std::sqrt(vv) / std::sqrt(ff) : 0.0;
+      for (size_t k = 0; k < n3; ++k) v[k] = (1.0 - alpha) * v[k] + sc * f[k];
+      if (n_pos > n_min) {
+        dt = std::min(dt * f_inc, dt_max);
+        alpha *= f_a;
+      }
+      ++n_pos;
+    } else {
+      std::fill(v.begin(), v.end(), 0.0);
+      dt *= f_dec;
+      alpha = a_start;
+      n_pos = 0;
+    }
+    double moved2 = 0.0;
+    for (int a = 0; a < n; ++a) {
+      double* va = &v[3 * (size_t)a];
+      const double* fa = &f[3 * (size_t)a];
+      for (int d = 0; d < 3; ++d) va[d] += fa[d] * dt;
+      const double sp = std::sqrt(va[0] * va[0] + va[1] * va[1] + va[2] * va[2]) * dt;
+      const double cap = sp > max_step ? max_step / sp : 1.0;
+      for (int d = 0; d < 3; ++d) {
+        va[d] *= cap;
+        x[3 * (size_t)a + d] += va[d] * dt;
+      }
+      const double ddx = x[3 * a] - xl[3 * a], ddy = x[3 * a + 1] - xl[3 * a + 1], ddz = x[3 * a + 2] - xl[3 * a + 2];
+      moved2 = std::max(moved2, ddx * ddx + ddy * ddy + ddz * ddz);
+    }
+    // A pair farther than rl at the build is farther than
+    // shrink·rl - 2·moved now, which must stay above the largest contact distance.
+    if (rl * shrink_since_build - 2.0 * std::sqrt(moved2) < dmax) build_pairs();
+  };
+  // compression: shrink_steps scale steps of equal ratio, relaxing in between
+  double total = 1.0;
+  if (reg.sphere) {
+    total = reg.r_target / reg.r_start;
+  } else {
+    total = (reg.hi1.x - reg.lo1.x) / (reg.hi0.x - reg.lo0.x);
+  }
+  const int shrink_steps = 160, relax_per_step = 3, max_final = 2000;
+  int it = 0;
+  build_pairs();
+  // the per-step ratio total^(1/shrink_steps) by bisection (only IEEE operations)
+  double ratio = 1.0;
+  if (total < 1.0) {
+    double lo_r = total, hi_r = 1.0;
+    for (int k = 0; k < 200; ++k) {
+      const double mid = 0.5 * (lo_r + hi_r);
+      double p = 1.0;
+      for (int q = 0; q < shrink_steps; ++q) p *= mid;
+      if (p < total) lo_r = mid; else hi_r = mid;
+    }
+    ratio = hi_r;
+    for (int k = 0; k < shrink_steps; ++k) {
+      scale_all(ratio);
+      for (int r = 0; r < relax_per_step; ++r, ++it) fire_step(false);
+    }
+  }
+  for (int k = 0; k < max_final; ++k, ++it) {
+    fire_step(true);
+    if (max_overlap < 0.1 && max_outside < 0.1) break;
+  }
+  // hydrogens onto their constraint lengths
+  for (const prismq_hcluster& c : T->clusters) {
+    const int ca = c.central_atom;
+    for (int h = 0; h < c.n_hydrogens; ++h) {
+      const int ha = c.hydrogen_atoms[h];
+      const double dx = x[3 * ha] - x[3 * ca], dy = x[3 * ha + 1] - x[3 * ca + 1], dz = x[3 * ha + 2] - x[3 * ca + 2];
+      const double r = std::sqrt(dx * dx + dy * dy + dz * dz);
+      if (r < 1e-9) continue;
+      const double s = (double)c.bond_lengths[h] / r;
+      x[3 * ha] = x[3 * ca] + dx * s;
+      x[3 * ha + 1] = x[3 * ca + 1] + dy * s;
+      x[3 * ha + 2] = x[3 * ca + 2] + dz * s;
+    }
+  }
+  for (size_t k = 0; k < x.size(); ++k) T->positions[k] = (float)x[k];
+  if (rep) {
+    rep->iterations = it;
+    rep->max_overlap = max_overlap;
+    rep->max_outside = max_outside;
+    build_pairs();
+    double mn = 1e300;
+    for (size_t p = 0; p < pi_.size(); ++p) {
+      const int i = pi_[p], j = pj_[p];
+      const double dx = x[3 * j] - x[3 * i], dy = x[3 * j + 1] - x[3 * i + 1], dz = x[3 * j + 2] - x[3 * i + 2];
+      mn = std::min(mn, std::sqrt(dx * dx + dy * dy + dz * dz));
+    }
+    rep->min_nonbonded = pi_.empty() ? 0.0 : mn;
+  }
+}
+
+// Default target density of the compacted systems: 2,500 atoms in a 40 Å
+// globule (a sphere of radius 20 Å).
+constexpr double kGlobuleDensity = 2500.0 / (4.0 / 3.0 * det::kPi * 8000.0);
+// Density at which the chains are grown before they are squeezed.
+constexpr double kGrowDensity = 0.02;
+
 bool polyala_build(int n_chains, int n_res, uint64_t seed, double density, double box_edge,
-                   HostTopology* T, std::string* err) {
+                   HostTopology* T, std::string* err, int compact, double* squeeze_stats) {
   if (n_chains < 1 || n_res < 1 || n_chains > 100000 || (long long)n_chains * n_res * 10 > 50000000LL) {
     *err = "polyala_build: n_chains/n_residues out of range";
     return false;
   }
-  if (!(density > 0.0)) density = 0.03;
+  if (!(density > 0.0)) density = compact ? kGlobuleDensity : kGrowDensity;
   const int atoms_per_chain = n_res * 10;
+  const double n_total = (double)n_chains * atoms_per_chain;
+  // Compacted systems grow at kGrowDensity in an enlarged region first.
+  double grow_density = density, grow_box = box_edge;
+  if (compact) {
+    grow_density = std::min(density, kGrowDensity);
+    if (box_edge > 0.0) grow_box = std::max(box_edge, det::cbrt(n_total / kGrowDensity));
+  }
   // A region that is too dense for self-avoiding growth is enlarged by 5% in
   // radius (or edge) per attempt.
   for (int attempt = 0; attempt < 16; ++attempt) {
@@ -668,27 +1007,57 @@ bool polyala_build(int n_chains, int n_res, uint64_t seed, double density, doubl
     const double grow = 1.0 + 0.05 * attempt;
     bool ok = true;
     int gx = 1, gy = 1, gz = 1;
-    if (box_edge > 0.0) split_box(n_chains, &gx, &gy, &gz);
+    if (grow_box > 0.0) split_box(n_chains, &gx, &gy, &gz);
+    SqueezeRegion sq;
+    sq.sphere = !(grow_box > 0.0);
     for (int c = 0; c < n_chains && ok; ++c) {
       Region reg;
-      if (box_edge > 0.0) {
+      if (grow_box > 0.0) {
         const int cx = c % gx, cy = (c / gx) % gy, cz = c / (gx * gy);
-        const double edge = box_edge * grow;
+        const double edge = grow_box * grow;
         const double ex = edge / gx, ey = edge / gy, ez = edge / gz;
         reg.sphere = false;
         reg.lo = {cx * ex, cy * ey, cz * ez};
         reg.hi = {(cx + 1) * ex, (cy + 1) * ey, (cz + 1) * ez};
+        if (compact) {
+          // the chain may use the whole cube; its slot only biases the growth
+          reg.has_pull = true;
+          reg.pull = 0.5 * (reg.lo + reg.hi);
+          reg.pull_scale = 0.5 * std::max(ex, std::max(ey, ez));
+          reg.lo = {0.0, 0.0, 0.0};
+          reg.hi = {edge, edge, edge};
+        }
+        if (c == 0) {
+          sq.lo0 = {0.0, 0.0, 0.0};
+          sq.hi0 = {edge, edge, edge};
+          const double h = 0.5 * (edge - box_edge);
+          sq.lo1 = {h, h, h};
+          sq.hi1 = {h + box_edge, h + box_edge, h + box_edge};
+        }
       } else {
         reg.sphere = true;
-        const double vol = atoms_per_chain / density;
+        const double vol = atoms_per_chain / grow_density;
         reg.radius = grow * det::cbrt(3.0 * vol / (4.0 * det::kPi));
         // chains of a multi-chain sphere system are laid side by side along x
         reg.center = {c * (2.0 * reg.radius + 6.0), 0.0, 0.0};
+        sq.centre.push_back(reg.center);
+        sq.r_start = reg.radius;
+        sq.r_target = det::cbrt(3.0 * (atoms_per_chain / density) / (4.0 * det::kPi));
       }
       ok = grow_chain(B, c, n_res, c * n_res, reg, rng);
     }
     if (!ok) continue;
     assemble(B, n_chains, n_res, T);
+    if (compact) {
+      SqueezeReport rep;
+      squeeze(T, B.type, atoms_per_chain, sq, &rep);
+      if (squeeze_stats) {
+        squeeze_stats[0] = rep.iterations;
+        squeeze_stats[1] = rep.max_overlap;
+        squeeze_stats[2] = rep.max_outside;
+        squeeze_stats[3] = rep.min_nonbonded;
+      }
+    }
     return true;
   }
   *err = "polyala_build: could not grow the chain(s) without clashes";

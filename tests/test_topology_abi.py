@@ -116,3 +116,79 @@ def test_box_mode_keeps_chains_in_their_cells(pq):
     p = t.positions
     assert p.min() >= -1e-3
     assert t.n_atoms == 800
+
+
+def _nonbonded_min_distance(t) -> float:
+    """Closest pair of atoms that are more than three bonds apart."""
+    from scipy.spatial import cKDTree
+
+    p = t.positions.astype(np.float64)
+    pairs = cKDTree(p).query_pairs(2.5, output_type="ndarray")
+    if len(pairs) == 0:
+        return 99.0
+    off, lst = t.exclusion_offsets, t.exclusions
+    keep = np.array([b not in lst[off[a]:off[a + 1]] for a, b in pairs])
+    if not keep.any():
+        return 99.0
+    d = np.linalg.norm(p[pairs[keep, 0]] - p[pairs[keep, 1]], axis=1)
+    return float(d.min())
+
+
+def _bond_errors(t):
+    p = t.positions.astype(np.float64)
+    b = t.bonds
+    r = np.linalg.norm(p[b["j"]] - p[b["i"]], axis=1)
+    heavy = np.abs(r - b["r0"]) / b["r0"]
+    c = t.clusters
+    h_err = 0.0
+    for k in range(3):
+        h = c["hydrogen_atoms"][:, k]
+        ok = h >= 0
+        rr = np.linalg.norm(p[h[ok]] - p[c["central_atom"][ok]], axis=1)
+        h_err = max(h_err, float(np.max(np.abs(rr - c["bond_lengths"][ok, k]) / c["bond_lengths"][ok, k])))
+    return float(heavy.max()), h_err
+
+
+def test_compact_globule_has_the_configured_size(pq):
+    """2,500 atoms collapsed into a 40 Å globule (0.0746 atoms/Å^3) with no
+    clash: atoms more than three bonds apart stay >= 1.5 Å apart, bonds keep
+    their lengths and the hydrogens sit on their constraint lengths."""
+    st = {}
+    t = pq.Topology.polyala_compact(1, 250, seed=5, stats=st)
+    p = t.positions.astype(np.float64)
+    assert t.n_atoms == 2500
+    ext = p.max(axis=0) - p.min(axis=0)
+    assert ext.max() <= 40.5, ext
+    rg = float(np.sqrt(((p - p.mean(axis=0)) ** 2).sum(axis=1).mean()))
+    assert 13.5 <= rg <= 16.5, rg
+    assert st["max_outside"] < 0.1 and st["max_overlap"] < 0.11
+    assert _nonbonded_min_distance(t) >= 1.5
+    heavy, h = _bond_errors(t)
+    assert heavy < 0.05 and h < 5e-6  # float32 rounding of the coordinates
+    # same chain, same bonded terms as the grown chain of the same seed
+    g = pq.Topology.polyala(1, 250, seed=5)
+    for f in ("bonds", "angles", "dihedrals", "exceptions", "clusters", "exclusions", "charges", "masses"):
+        assert np.array_equal(getattr(t, f), getattr(g, f)), f
+
+
+def test_compact_box_packs_every_chain_inside(pq):
+    """Chains packed into one cube (the 40-chain, 110 Å system at a smaller
+    size: 4 chains of 50 residues in a 29.9 Å cube, 0.0749 atoms/Å^3)."""
+    edge = 29.9
+    st = {}
+    t = pq.Topology.polyala_compact(4, 50, seed=8, box_edge=edge, stats=st)
+    p = t.positions.astype(np.float64)
+    ext = p.max(axis=0) - p.min(axis=0)
+    assert ext.max() <= edge + 0.25, ext
+    assert ext.min() >= edge - 3.0, ext
+    assert _nonbonded_min_distance(t) >= 1.5
+    heavy, h = _bond_errors(t)
+    assert heavy < 0.05 and h < 5e-6  # float32 rounding of the coordinates
+
+
+def test_compact_generator_is_deterministic(pq):
+    a = pq.Topology.polyala_compact(1, 40, seed=42)
+    b = pq.Topology.polyala_compact(1, 40, seed=42)
+    c = pq.Topology.polyala_compact(1, 40, seed=43)
+    assert np.array_equal(a.positions, b.positions)
+    assert not np.array_equal(a.positions, c.positions)
