@@ -3,20 +3,29 @@
 
 Default workload: the batched ensemble — 256 independent seeded poly-alanine
 systems, chain lengths log-uniform in 50–800 residues (500–8,000 atoms), each
-with its own Philox stream, advanced together (one launch per phase, CUDA
-graph).  One "step" is one MD step of every resident system.
+chain collapsed into a globule at 0.0746 atoms/Å^3 (2,500 atoms in 40 Å) and
+given its own Philox stream, advanced together (one launch per phase, CUDA
+graph).  One "step" is one MD step of every resident system.  --workload
+large100k is the single 100,000-atom system (40 chains packed in a 110 Å
+cube), plain2500 one 2,500-atom globule, serve the Poisson job stream,
+precision the FP32-vs-FP64 study.
 
 Printed (rank 0, one JSON line): value = whole-job device throughput with the
 state resident in HBM (CUDA events on the library's stream around a graph of K
 steps); e2e = the same metric through the C ABI with host state uploaded from
-pinned memory and read back every step; roofline of the force kernel (CUDA
-events around every force launch inside the timed graph); the plain
+pinned memory and read back every step; the roofline of the force kernel (its
+average duration launched alone over every system, CUDA events); the plain
 one-system-at-a-time loop on a stratified sample of the same systems; the CPU
-baseline (the oracle's restatement of the reference step, all host threads).
+baseline (the oracle's restatement of the reference step, all host threads)
+on a stratified sample at the device arm's equilibrated states.
+
+--gpus N without a launcher starts N ranks through torch.distributed.run;
+systems are sharded round-robin over the ranks with no data-path collective.
 
 --impl reference times the reference's CPU step (oracle restatement; the
-reference ships no CPU implementation and its Rust host cannot be built) on a
-stratified sample of the same workload.
+reference ships no CPU implementation and its Rust host cannot be built) on
+the same stratified sample, with inputs from the oracle's own build of the
+generator: the product library is not loaded.
 """
 from __future__ import annotations
 
@@ -40,7 +49,6 @@ ROOT = pathlib.Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "aggregate atom-steps/s, batched vs plain, 1 GB300; p50/p99 job latency"
-FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12  # SMs x FP32 lanes x FMA x max SM clock
 
 
 def args_parse():
@@ -56,20 +64,27 @@ def args_parse():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--equil", type=int, default=400,
-                    help="MD steps run on the freshly grown systems before warm-up (equilibration)")
+                    help="MD steps run on the freshly built systems before warm-up (equilibration)")
+    ap.add_argument("--cpu-systems", type=int, default=16,
+                    help="stratified systems of the workload that the CPU legs time")
+    ap.add_argument("--cpu-steps", type=int, default=20, help="steps the device arm's CPU-baseline leg times")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving leg of the default run")
     ap.add_argument("--serve-jobs", type=int, default=200)
     ap.add_argument("--serve-rate", type=float, default=50.0, help="Poisson arrival rate, jobs/s")
     ap.add_argument("--serve-hbm-gb", type=float, default=16.0, help="device bytes of the server arena")
-    ap.add_argument("--serve-pool", type=int, default=24, help="distinct seeded topologies the jobs draw from")
+    ap.add_argument("--serve-pool", type=int, default=64, help="distinct seeded topologies the jobs draw from")
     ap.add_argument("--drift-systems", type=int, default=16, help="precision study: systems in the drift runs")
     ap.add_argument("--drift-steps", type=int, default=2500, help="precision study: steps of each drift run")
     return ap.parse_args()
 
 
 # ------------------------------------------------------------------ workload
+# Atom density of the collapsed chains: 2,500 atoms in a 40 Å globule.
+GLOBULE_DENSITY = 2500.0 / (4.0 / 3.0 * math.pi * 20.0 ** 3)
+
+
 def workload_sizes(kind: str, nsys: int, seed: int) -> list[tuple[int, int, float]]:
-    """(n_chains, n_residues, box_edge) per system."""
+    """(n_chains, n_residues, box_edge) per system; box_edge 0 = one globule per chain."""
     if kind == "plain2500":
         return [(1, 250, 0.0)]
     if kind == "large100k":
@@ -79,25 +94,58 @@ def workload_sizes(kind: str, nsys: int, seed: int) -> list[tuple[int, int, floa
     return [(1, int(round(r)), 0.0) for r in res]
 
 
-def build_topologies(pq, specs, indices, seed):
+def workload_config(args, specs) -> dict:
+    """The workload as both arms describe it (inputs only, nothing measured)."""
+    geometry = {
+        "batch256": "each chain (log-uniform 50-800 residues) collapsed into a globule at %.4f atoms/A^3" % GLOBULE_DENSITY,
+        "plain2500": "one 250-residue chain collapsed into a 40 A globule (%.4f atoms/A^3)" % GLOBULE_DENSITY,
+        "large100k": "40 chains x 250 residues packed in a 110 A cube (0.0751 atoms/A^3)",
+    }.get(args.workload, args.workload)
+    return {"workload": args.workload, "systems": len(specs),
+            "atoms_total": int(sum(10 * c * r for c, r, _ in specs)), "geometry": geometry,
+            "dt_ps": 0.004, "cutoff_A": 10.0, "skin_A": 2.0, "rebuild_interval": 20, "gamma_per_ps": 1.0,
+            "temperature_K": 300.0, "hmr": "H 3.024 amu", "equilibration_steps": args.equil,
+            "seed": args.seed, "parallelism": f"independent systems sharded over {args.gpus} GPU(s)",
+            "l2": "inputs larger than L2 (state + neighbour lists of 10^5-10^6 atoms, re-read every step)"}
+
+
+def system_seed(seed: int, i: int) -> int:
+    return seed + 7919 * i
+
+
+def build_topologies(gen, specs, indices, seed):
+    """gen(n_chains, n_residues, seed, box_edge) -> topology, on a thread pool
+    (the generator releases the interpreter while it runs)."""
     def one(i):
         c, r, box = specs[i]
-        return pq.Topology.polyala(c, r, seed=seed + 7919 * i, box_edge=box)
+        return gen(c, r, system_seed(seed, i), box)
 
     with ThreadPoolExecutor(max_workers=min(32, os.cpu_count() or 4)) as ex:
         return list(ex.map(one, indices))
 
 
+def library_generator(pq):
+    return lambda c, r, seed, box: pq.Topology.polyala_compact(c, r, seed=seed, box_edge=box)
+
+
+def oracle_generator():
+    from oracle import oracle as orc
+
+    return lambda c, r, seed, box: orc.polyala(c, r, seed, box_edge=box, compact=True)
+
+
 def pair_stats(topo) -> dict:
-    """Unique ordinary pairs within 10 Å (P10) and bonded term counts."""
+    """Unique ordinary pairs within 10 Å (P10) and 12 Å (list entries), and bonded term counts."""
     from scipy.spatial import cKDTree
 
     p = topo.positions.astype(np.float64)
     t = cKDTree(p)
     within = (int(t.count_neighbors(t, 10.0)) - len(p)) // 2
+    within12 = (int(t.count_neighbors(t, 12.0)) - len(p)) // 2
     excl = len(topo.exclusions) // 2
-    return {"atoms": topo.n_atoms, "p10": max(within - excl, 0), "bonds": len(topo.bonds),
-            "angles": len(topo.angles), "dihedrals": len(topo.dihedrals), "exceptions": len(topo.exceptions)}
+    return {"atoms": topo.n_atoms, "p10": max(within - excl, 0), "p12": max(within12 - excl, 0),
+            "bonds": len(topo.bonds), "angles": len(topo.angles), "dihedrals": len(topo.dihedrals),
+            "exceptions": len(topo.exceptions)}
 
 
 def flops_per_step(st: dict) -> float:
@@ -107,9 +155,21 @@ def flops_per_step(st: dict) -> float:
             90.0 * st["dihedrals"] + 60.0 * st["atoms"])
 
 
-def bytes_per_step(st: dict, list_len: float = 0.0) -> float:
-    # x (16) + v r/w (32) + int64 forces w/r (48) + per-atom params (16) + x_start (16) per atom
-    return st["atoms"] * (128.0 + 4.0 * list_len / 20.0)
+def bytes_per_step(st: dict, steps_per_build: float) -> float:
+    # x (16) + v r/w (32) + int64 forces w/r (48) + per-atom params (16) +
+    # x_start (16) per atom, plus the list: 4 bytes per entry (both ends of
+    # every pair within the 12 Å list radius) written once per build
+    return st["atoms"] * 128.0 + 4.0 * 2.0 * st["p12"] / max(steps_per_build, 1.0)
+
+
+def maxwell_boltzmann(topo, temperature: float, seed: int) -> np.ndarray:
+    """Seeded velocities (Å/ps) at `temperature`, centre-of-mass motion removed."""
+    kb = 0.0019872041  # kcal/(mol K)
+    m = topo.masses.astype(np.float64)
+    rng = np.random.default_rng(seed)
+    v = rng.standard_normal((topo.n_atoms, 3)) * np.sqrt(418.4 * kb * temperature / m)[:, None]
+    v -= (m[:, None] * v).sum(axis=0) / m.sum()
+    return v.astype(np.float32)
 
 
 # ------------------------------------------------------------------ clocks
@@ -164,14 +224,35 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------ distributed
-def dist_setup(n_gpus: int):
+def spawn_ranks(n: int, argv: list[str]) -> int:
+    """Run this script as n ranks through torch.distributed.run on 127.0.0.1
+    (used when --gpus N > 1 is given without a launcher); returns the exit code."""
+    import socket
+
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes", "1", "--nproc-per-node", str(n),
+           "--master-addr", "127.0.0.1", "--master-port", str(port), *argv]
+    return subprocess.run(cmd).returncode
+
+
+def dist_setup(n_gpus: int, pq=None):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world != n_gpus:
+        raise SystemExit(f"--gpus {n_gpus} but WORLD_SIZE {world}")
     import torch
 
     if torch.cuda.is_available():
         torch.cuda.set_device(local)
+    if pq is not None:
+        # the library's CUDA runtime is its own: select its device too, and check it
+        pq.set_device(local)
+        if pq.device_ordinal() != local:
+            raise SystemExit(f"rank {rank}: library device {pq.device_ordinal()} != LOCAL_RANK {local}")
     if world > 1:
         import torch.distributed as dist
 
@@ -186,26 +267,30 @@ def barrier(world):
         dist.barrier()
 
 
-def max_over_ranks(v: float, world: int) -> float:
-    if world == 1:
-        return v
+def _reduce(v: float, world: int, op) -> float:
     import torch
     import torch.distributed as dist
 
-    t = torch.tensor([v], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=op)
     return float(t.item())
+
+
+def max_over_ranks(v: float, world: int) -> float:
+    if world == 1:
+        return v
+    import torch.distributed as dist
+
+    return _reduce(v, world, dist.ReduceOp.MAX)
 
 
 def sum_over_ranks(v: float, world: int) -> float:
     if world == 1:
         return v
-    import torch
     import torch.distributed as dist
 
-    t = torch.tensor([v], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
-    return float(t.item())
+    return _reduce(v, world, dist.ReduceOp.SUM)
 
 
 # ------------------------------------------------------------------ CPU legs
@@ -215,50 +300,54 @@ def stratified(n: int, k: int) -> list[int]:
     return sorted({int(round(i * (n - 1) / (k - 1))) for i in range(k)})
 
 
-def cpu_reference_rate(pq, topos, steps_cap: int, seconds: float, threads: int) -> tuple[float, str]:
-    """Oracle restatement of the reference step loop; returns atom-steps/s."""
+def cpu_step_rate(systems, steps: int, threads: int) -> tuple[float, float, str]:
+    """The oracle's restatement of the reference step loop (per-step REF27
+    rebuild, two FP32 force evaluations per step, OpenMP over `threads`).
+    One step = one MD step of every system of the sample, in turn.
+    systems: [(topology, x, v)].  Returns (atom-steps/s, ms per step, sample)."""
     from oracle import oracle as orc
 
     orc.build()
-    p = pq.Params()
-    atoms_steps, wall = 0, 0.0
-    desc = []
-    budget = seconds / max(len(topos), 1)
-    for t in topos:
-        o = orc.OracleSystem(t.struct(), seed=p.seed, stream=p.stream)
-        eng_v = np.zeros((t.n_atoms, 3), np.float32)
-        o.set_state(t.positions, eng_v)
-        t0 = time.perf_counter()
-        o.run(1, threads)
-        one = max(time.perf_counter() - t0, 1e-4)
-        n = int(max(1, min(steps_cap, budget / one)))
-        t0 = time.perf_counter()
-        rc = o.run(n, threads)
-        dt = time.perf_counter() - t0
-        if rc:
-            raise RuntimeError(f"oracle step failed ({rc})")
-        atoms_steps += t.n_atoms * n
-        wall += dt
-        desc.append(f"{t.n_atoms}x{n}")
+    objs = []
+    for t, x, v in systems:
+        o = orc.OracleSystem(t.struct())
+        o.set_state(x, v)
+        objs.append(o)
+    atoms = sum(t.n_atoms for t, _, _ in systems)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for o in objs:
+            rc = o.run(1, threads)
+            if rc:
+                raise RuntimeError(f"oracle step failed ({rc})")
+    wall = time.perf_counter() - t0
+    for o in objs:
         o.close()
-    return atoms_steps / wall, ", ".join(desc)
+    desc = f"{len(systems)} stratified systems ({atoms} atoms: " + ", ".join(str(t.n_atoms) for t, _, _ in systems) + ")"
+    return atoms * steps / wall, wall * 1e3 / steps, desc
 
 
 # ------------------------------------------------------------------ serving
 def run_serving(args, pq) -> dict:
     """Poisson stream of MD jobs through the job server (prismq_server_*).
 
-    Jobs: atoms log-uniform in [300, 20000] (chains of 30-2000 residues drawn
-    from a pool of seeded topologies at stratified sizes), steps uniform in
-    [500, 5000], arrivals Poisson at --serve-rate.  Every job has its own noise
-    stream.  Latency = submit -> final state written to the job's host buffers.
+    Jobs: chains of 30-2,000 residues (300-20,000 atoms, log-uniform), each
+    collapsed into a globule, drawn from a pool of --serve-pool seeded
+    topologies at stratified sizes; steps uniform in [500, 5000]; arrivals
+    Poisson at --serve-rate; every job has its own noise stream and starting
+    velocities.  Latency = submit -> final state written to the job's host
+    buffers.  The steady-state rate counts the atom-steps done inside the
+    middle 60 % of the arrival span, each job's steps spread evenly over its
+    residence in the arena.
     """
     rng = np.random.default_rng(args.seed + 4)
     P = args.serve_pool
     lo, hi = math.log(30), math.log(2000)
     residues = [int(round(math.exp(lo + (i + 0.5) / P * (hi - lo)))) for i in range(P)]
     specs = [(1, r, 0.0) for r in residues]
-    pool = build_topologies(pq, specs, list(range(P)), args.seed + 17)
+    t_gen = time.perf_counter()
+    pool = build_topologies(library_generator(pq), specs, list(range(P)), args.seed + 17)
+    t_gen = time.perf_counter() - t_gen
     n = args.serve_jobs
     pick = rng.integers(0, P, size=n)
     steps = rng.integers(500, 5001, size=n)
@@ -280,7 +369,7 @@ def run_serving(args, pq) -> dict:
                 break
             results += srv.poll(wait_ms=max(1, int(wait * 1000)))
         srv.submit(pool[pick[k]], int(steps[k]), pq.Params(stream=k), tag=k)
-    t_end = time.time() + 600
+    t_end = time.time() + 3600
     while len(results) < n and time.time() < t_end:
         results += srv.poll(wait_ms=200)
     st = srv.stats()
@@ -292,8 +381,15 @@ def run_serving(args, pq) -> dict:
     last = max(r.end_s for r in results)
     atom_steps = float(sum(r.n_atoms * r.steps_done for r in ok))
     atoms = np.array([pool[i].n_atoms for i in pick])
+    w0, w1 = first + 0.2 * (arrivals[-1] - arrivals[0]), first + 0.8 * (arrivals[-1] - arrivals[0])
+    mid = 0.0
+    for r in ok:
+        span = max(r.end_s - r.start_s, 1e-9)
+        overlap = max(0.0, min(r.end_s, w1) - max(r.start_s, w0))
+        mid += r.n_atoms * r.steps_done * overlap / span
     return {
         "value": atom_steps / (last - first), "unit": "atom-steps/s",
+        "steady_state_atom_steps_per_s": mid / max(w1 - w0, 1e-9),
         "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                       "mean": float(lat.mean()), "max": float(lat.max())},
         "queue_wait_s": {"p50": float(np.percentile(wait, 50)), "p99": float(np.percentile(wait, 99))},
@@ -304,8 +400,8 @@ def run_serving(args, pq) -> dict:
         "offered_atom_steps_per_s": float((atoms * steps).sum() / arrivals[-1]),
         "gpu_busy_frac": (st["busy_s"] - base["busy_s"]) / max(last - first, 1e-9),
         "chunks": st["chunks"] - base["chunks"], "arena_atoms": st["capacity_atoms"],
-        "arena_bytes": st["device_bytes"],
-        "sample": f"{n} jobs from a pool of {P} seeded chains (30-2000 residues), Poisson arrivals",
+        "arena_bytes": st["device_bytes"], "pool_build_s": t_gen,
+        "sample": f"{n} jobs drawn from a pool of {P} seeded compact chains (30-2000 residues), Poisson arrivals",
     }
 
 
@@ -317,7 +413,7 @@ def run_precision(args, pq) -> dict:
     identity (stratified subset), constraint error with SHAKE at 1e-6."""
     specs = workload_sizes("batch256", args.systems, args.seed)
     idx = list(range(len(specs)))
-    topos = build_topologies(pq, specs, idx, args.seed)
+    topos = build_topologies(library_generator(pq), specs, idx, args.seed)
     atoms = sum(t.n_atoms for t in topos)
     F32, F64 = pq.PRECISION_FP32, pq.PRECISION_FP64
     # ---- force error at identical positions, every system
@@ -428,39 +524,79 @@ def _bond_err(topo, x) -> float:
 
 
 # ------------------------------------------------------------------ main legs
-def run_reference(args, pq, rank, world):
+def cpu_sample(args, specs) -> list[int]:
+    """Indices of the stratified systems both CPU legs time."""
+    return stratified(len(specs), args.cpu_systems)
+
+
+def run_reference(args, rank, world):
+    """The reference's CPU implementation of the step (the oracle's
+    restatement; the reference ships no CPU path and its Rust host cannot be
+    built here) on the host cores.  Inputs come from the oracle's own build of
+    the generator, so the product library is not loaded; the sampled systems
+    start from Maxwell-Boltzmann velocities and are equilibrated for --equil
+    steps by the same CPU step before warm-up and timing."""
     if rank != 0:
         return
     specs = workload_sizes(args.workload, args.systems, args.seed)
-    idx = stratified(len(specs), 4 if args.workload == "batch256" else 1)
-    topos = build_topologies(pq, specs, idx, args.seed)
+    idx = cpu_sample(args, specs)
+    topos = build_topologies(oracle_generator(), specs, idx, args.seed)
     threads = os.cpu_count() or 1
-    cpu_reference_rate(pq, topos[:1], 2, 1.0, threads)  # warm-up: page in, spin up the thread pool
-    value, desc = cpu_reference_rate(pq, topos, max(args.steps, 1), 30.0, threads)
+    from oracle import oracle as orc
+
+    states = []
+    for i, t in zip(idx, topos):
+        o = orc.OracleSystem(t.struct(), stream=i)
+        o.set_state(t.positions, maxwell_boltzmann(t, 300.0, system_seed(args.seed, i)))
+        if o.run(args.equil + args.warmup, threads):
+            raise RuntimeError("oracle equilibration failed")
+        x, v = o.get_state()
+        o.close()
+        states.append((t, x, v))
+    value, ms, desc = cpu_step_rate(states, max(args.steps, 1), threads)
     line = {"metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "higher_is_better": True, "impl": "reference", "dtype": "f32",
-            "data": "synthetic (seeded poly-alanine systems)",
-            "config": {"workload": args.workload, "systems_sampled": len(topos), "sample": desc},
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "impl": "reference",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded compact poly-alanine systems; no dataset)",
+            "config": workload_config(args, specs),
             "cpu_baseline": {"value": value, "unit": "atom-steps/s", "cores": threads, "kind": "port",
-                             "sample": f"oracle restatement of the reference step loop on {desc} (atoms x steps)"},
+                             "sample": f"oracle restatement of the reference step loop (per-step REF27 rebuild, "
+                                       f"two FP32 force evaluations per step) on {desc}, each equilibrated "
+                                       f"{args.equil} steps; one step = one step of every sampled system"},
             "e2e": {"value": value, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "vs_baseline": None}
+            "gpu_launches": 0}
     print(json.dumps(line), flush=True)
+
+
+def force_traffic(cfg: dict) -> tuple[float | None, str | None]:
+    """DRAM bytes per force launch from the committed ncu summary of this
+    workload, if one exists for it (same workload and atom count)."""
+    for f in sorted((ROOT / "profiles").glob("k_force_*.txt")):
+        kv = {}
+        for ln in f.read_text().splitlines():
+            parts = ln.split()
+            if len(parts) >= 2 and not ln.startswith("#"):
+                kv[parts[0]] = parts[1]
+        if kv.get("workload") == cfg["workload"] and kv.get("atoms_total") == str(cfg["atoms_total"]) \
+                and "dram_bytes_per_launch" in kv:
+            return float(kv["dram_bytes_per_launch"]), str(f.relative_to(ROOT))
+    return None, None
 
 
 def run_ours(args, pq, rank, world):
     import torch
 
     specs = workload_sizes(args.workload, args.systems, args.seed)
+    cfg = workload_config(args, specs)
     mine = [i for i in range(len(specs)) if i % world == rank]
-    topos = build_topologies(pq, specs, mine, args.seed)
+    topos = build_topologies(library_generator(pq), specs, mine, args.seed)
     atoms = sum(t.n_atoms for t in topos)
     batch = pq.Batch(max_atoms=atoms + 64 * len(topos), max_systems=len(topos))
     slots = []
     for i, t in zip(mine, topos):
         slots.append(batch.add_system(t, pq.Params(stream=i)))
     if args.equil > 0:
-        batch.step(args.equil)  # leave the transient right after growth
+        batch.step(args.equil)  # leave the transient right after the compaction
     batch.step(max(args.warmup, 3))
     rebuilds0 = sum(batch.counters(s)[1] for s in slots)
     # pair statistics at the warmed-up positions
@@ -506,6 +642,8 @@ def run_ours(args, pq, rank, world):
         raise pq.PrismQError(rc, pq.load().prismq_last_error().decode())
     f_avg_ms = f_ms.value
     achieved = flops_launch / (f_avg_ms / 1e3) / 1e12
+    dev = pq.device_info()
+    fp32_peak = dev["sms"] * 128 * 2 * dev["sm_clock_khz"] * 1e3 / 1e12
     # ---------------- e2e through the C ABI with pinned host buffers
     span = int(pq.load().prismq_batch_atom_span(batch.h))
     hx = torch.empty(3 * span, dtype=torch.float32, pin_memory=True).numpy()
@@ -531,6 +669,9 @@ def run_ours(args, pq, rank, world):
         a_sum, t_sum = 0, 0.0
         for k in pick:
             eng = pq.NhsAmberFusedEngine(topos[k], pq.Params(stream=mine[k]))
+            x, v = batch.get_state(slots[k])
+            eng.set_positions(x)
+            eng.set_velocities(v)
             eng.step(3)
             n = 200
             torch.cuda.synchronize()
@@ -541,48 +682,46 @@ def run_ours(args, pq, rank, world):
             t_sum += dt
             eng.close()
         plain_value = a_sum / t_sum
-    # ---------------- CPU baseline (rank 0, N = 1)
+    # ---------------- CPU baseline (rank 0, N = 1) on the equilibrated states
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        pick = stratified(len(topos), 3)
+        idx = cpu_sample(args, specs)
         threads = os.cpu_count() or 1
-        rate, desc = cpu_reference_rate(pq, [topos[k] for k in pick], 400, 20.0, threads)
+        systems = [(topos[i], *batch.get_state(slots[i])) for i in idx]
+        rate, _, desc = cpu_step_rate(systems, args.cpu_steps, threads)
         cpu = {"value": rate, "unit": "atom-steps/s", "cores": threads, "kind": "port",
                "sample": f"oracle restatement of the reference step loop (per-step REF27 rebuild, two FP32 force "
-                         f"evaluations per step), systems atoms x steps: {desc}"}
-    traffic = None
-    tf = ROOT / "profiles" / "force_traffic.txt"
-    if tf.exists():
-        for ln in tf.read_text().splitlines():
-            if ln.startswith("dram_bytes_per_atom_step"):
-                traffic = float(ln.split()[1]) * atoms
-    roof = {"bound": "fp32", "achieved": achieved, "peak": FP32_PEAK_TFLOPS, "unit": "TFLOP/s",
-            "frac": achieved / FP32_PEAK_TFLOPS, "traffic": traffic,
-            "peak_source": "nominal FP32 SIMT peak (152 SMs x 128 lanes x 2 x 2.07 GHz); MEASURED_PEAKS has no FP32 entry",
+                         f"evaluations per step) on {desc} at the device arm's equilibrated states, "
+                         f"{args.cpu_steps} steps"}
+    traffic, traffic_src = force_traffic(cfg)
+    roof = {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+            "frac": achieved / fp32_peak, "traffic": traffic, "traffic_source": traffic_src,
+            "peak_source": f"FP32 SIMT peak of the device: {dev['sms']} SMs x 128 lanes x 2 (FMA) x "
+                           f"{dev['sm_clock_khz'] / 1e3:.0f} MHz peak SM clock (MEASURED_PEAKS has no FP32 entry)",
             "kernel": "k_force", "kernel_avg_ms": f_avg_ms, "flops_per_launch": flops_launch}
     try:
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
-        hbm_peak = float(peaks["hbm_gbs"])
+        hbm_peak, hbm_src = float(peaks["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs"
     except (OSError, ValueError, KeyError):
-        hbm_peak = 6800.0
-    step_bytes = sum(bytes_per_step(s) for s in stats)
-    hbm = {"achieved_gbs": step_bytes * args.steps / t_max / 1e9, "peak_gbs": hbm_peak,
-           "frac": step_bytes * args.steps / t_max / 1e9 / hbm_peak}
+        hbm_peak, hbm_src = 6800.0, "fallback 6.8 TB/s"
+    step_bytes = sum(bytes_per_step(s, steps_per_build) for s in stats)
+    hbm = {"achieved_gbs": step_bytes * args.steps / t_max / 1e9, "peak_gbs": hbm_peak, "peak_source": hbm_src,
+           "frac": step_bytes * args.steps / t_max / 1e9 / hbm_peak,
+           "bytes_per_step": step_bytes}
     line = {
         "metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded poly-alanine systems; no dataset)",
-        "config": {"workload": args.workload, "systems": len(specs), "atoms_total": int(total_atoms),
-                   "atoms_rank0": atoms, "p10_per_atom": p10_mean, "equilibration_steps": args.equil,
-                   "steps_per_list_build": steps_per_build, "force_launch_shape": batch.tuning(),
-                   "parallelism": f"independent systems sharded over {world} GPU(s)",
-                   "l2": "inputs larger than L2 (neighbour rows ~4 KiB/atom, re-read every step)"},
+        "data": "synthetic (seeded compact poly-alanine systems; no dataset)",
+        "config": cfg,
+        "measured": {"atoms_rank0": atoms, "p10_per_atom": p10_mean, "steps_per_list_build": steps_per_build,
+                     "force_launch_shape": batch.tuning(), "device": dev},
         "e2e": {"value": e2e_value, "unit": "atom-steps/s", "h2d_bytes_per_step": 24 * span,
                 "d2h_bytes_per_step": 24 * span, "steps": args.e2e_steps},
         "plain": None if plain_value is None else {"value": plain_value, "unit": "atom-steps/s",
                                                    "batched_over_plain": value / plain_value,
-                                                   "sample": "8 stratified systems run alone, 200 steps each"},
+                                                   "sample": "8 stratified systems run alone from their "
+                                                             "equilibrated states, 200 steps each"},
         "roofline": roof, "hbm": hbm, "kernel_avg_ms": phase_avg, "gpu_launches": int(launches), "clocks": clk,
         "cpu_baseline": cpu,
     }
@@ -595,14 +734,24 @@ def run_ours(args, pq, rank, world):
 
 def main():
     args = args_parse()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # no launcher: start the ranks here, one process per GPU
+        sys.exit(spawn_ranks(args.gpus, [str(pathlib.Path(__file__).resolve()), *sys.argv[1:]]))
+    if args.impl == "reference":
+        # host cores only: the product library is neither built nor loaded
+        rank, world, _ = dist_setup(args.gpus)
+        run_reference(args, rank, world)
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.destroy_process_group()
+        return
     import __graft_entry__
 
     __graft_entry__.build()
     pq = importlib.import_module("prism-q_gb300")
-    rank, world, _ = dist_setup(args.gpus)
-    if args.impl == "reference":
-        run_reference(args, pq, rank, world)
-    elif args.workload == "precision":
+    rank, world, _ = dist_setup(args.gpus, pq)
+    if args.workload == "precision":
         if rank == 0:
             t0 = time.perf_counter()
             pr = run_precision(args, pq)
@@ -610,7 +759,7 @@ def main():
                     "value": pr["force_rel_rms_fp32_vs_fp64_oracle"]["max"],
                     "unit": "relative RMS force error vs the FP64 oracle (max over systems)",
                     "n_gpus": 1, "higher_is_better": False, "dtype": "f32 vs f64",
-                    "data": "synthetic (seeded poly-alanine systems; no dataset)",
+                    "data": "synthetic (seeded compact poly-alanine systems; no dataset)",
                     "config": {"workload": "precision", "systems": args.systems, "equilibration_steps": args.equil},
                     "precision": pr, "wall_s": time.perf_counter() - t0}
             print(json.dumps(line), flush=True)
@@ -623,8 +772,10 @@ def main():
             clk = clocks.stop()
             line = {"metric": METRIC, "value": sv["value"], "unit": "atom-steps/s", "n_gpus": 1,
                     "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-                    "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded poly-alanine jobs; no dataset)",
+                    "vs_baseline": None, "dtype": "f32",
+                    "data": "synthetic (seeded compact poly-alanine jobs; no dataset)",
                     "config": {"workload": "serve", "jobs": sv["jobs"], "arrival_rate_per_s": sv["arrival_rate_per_s"],
+                               "pool": args.serve_pool, "hbm_gb": args.serve_hbm_gb,
                                "parallelism": "one job server on 1 GPU"},
                     "e2e": {"value": sv["value"], "unit": "atom-steps/s",
                             "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,

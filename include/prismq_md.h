@@ -144,6 +144,20 @@ int prismq_abi_version(void);
 int prismq_device_count(void);
 /* Kernels this library has launched in this process (graph nodes counted). */
 long long prismq_kernel_launches(void);
+/* The CUDA runtime is linked into this library, so its current device is its
+ * own: another framework's device selection (torch.cuda.set_device, ...) does
+ * not reach it.  A process that drives GPU k calls prismq_set_device(k) before
+ * it creates systems, batches or servers; handles live on the device that was
+ * current on the thread that created them and are used from threads that have
+ * the same device selected (a server's worker thread takes its creator's).
+ * No counterpart in the reference (one engine per process and stream).
+ * Applies to the calling thread. */
+prismq_status prismq_set_device(int32_t ordinal);
+/* The calling thread's current device in this library (-1 without a device). */
+int32_t prismq_device_ordinal(void);
+/* out = {ordinal, streaming multiprocessors, peak SM clock in kHz} of the
+ * calling thread's current device. */
+prismq_status prismq_device_info(int32_t out[3]);
 
 /* ---- synthetic poly-alanine-like systems (host only, no GPU) ---- */
 
@@ -554,15 +568,21 @@ void prismq_server_destroy(prismq_server* s);
  *   d_rows    device int32[n_atoms*row_cap]; row i holds its neighbours
  *   d_counts  device int32[n_atoms]; row lengths (-1 for a row that overflowed)
  *   stream    a cudaStream_t (NULL for the default stream)
- * Limits: 1 <= n_atoms <= 65536, 1 <= row_cap <= 1024, at most 512 atoms in a
- * cell (cells are at least list_radius/2 wide); larger sizes are rejected with
- * PRISMQ_E_CAPACITY before any GPU work.  The call calls no cudaMalloc or
- * cudaFree: its cell lists live in one fixed file-scope device array (about
- * 0.8 MB) that every GPU loading the library keeps until the process exits.
- * The first call on a device looks up that array's device address (set-up
- * work; make it before any stream capture).  Every call reuses the same array,
- * so calls that overlap on the GPU race and must be serialised by the caller.
- * The call returns after the stream has finished the work. */
+ * Limits: 1 <= n_atoms <= 65536 and 1 <= row_cap <= 1024, checked on the host
+ * and rejected with PRISMQ_E_CAPACITY before any GPU work.  Two limits are
+ * found on the GPU and reported after the work: a cell (cells are at least
+ * list_radius/2 wide) holding more than 512 atoms returns
+ * PRISMQ_E_CELL_OVERFLOW with every count set to -1, and a row longer than
+ * row_cap returns PRISMQ_E_NEIGHBOR_OVERFLOW with that row's count set to -1
+ * (nothing is written past row_cap; the other rows are complete).  The call
+ * calls no cudaMalloc or cudaFree: its cell lists live in one fixed file-scope
+ * device array (about 0.8 MB) that every GPU loading the library keeps until
+ * the process exits.  The first call on a device looks up that array's device
+ * address (set-up work; make it before any stream capture); the address is
+ * kept for the process, so the entry point must not be used across a
+ * cudaDeviceReset.  Every call reuses the same array, so calls that overlap on
+ * the GPU race and must be serialised by the caller.  The call synchronises
+ * the stream: it returns after the stream has finished the work. */
 prismq_status prismq_neighbor_rows_noalloc(const float* d_xyz, int32_t n_atoms, float list_radius,
                                            int32_t row_cap, int32_t* d_rows, int32_t* d_counts,
                                            void* stream);

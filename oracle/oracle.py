@@ -22,8 +22,15 @@ LIB = BUILD / "liboracle.so"
 FLAGS = ["-O2", "-std=c11", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared"]
 
 
+GEN_SRC = [HERE / "gen_shim.cpp", HERE.parent / "prism-q_gb300" / "csrc" / "topology.cpp"]
+GEN_LIB = BUILD / "liboracle_gen.so"
+GEN_FLAGS = ["-O3", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared"]
+
+
 def build(force: bool = False) -> pathlib.Path:
-    """Compile the oracle with gcc (no contraction, OpenMP)."""
+    """Compile the oracle with gcc (no contraction, OpenMP), and its build of
+    the input generator (build_gen)."""
+    build_gen(force)
     deps = [SRC, HDR, HERE.parent / "include" / "prismq_md.h"]
     if not force and LIB.exists() and all(LIB.stat().st_mtime >= d.stat().st_mtime for d in deps):
         return LIB
@@ -35,6 +42,62 @@ def build(force: bool = False) -> pathlib.Path:
         raise RuntimeError(f"oracle build failed:\n{res.stderr}")
     os.replace(tmp, LIB)
     return LIB
+
+
+def build_gen(force: bool = False) -> pathlib.Path:
+    """The library's synthetic-system generator (host C++) compiled into the
+    oracle's own shared object, so CPU legs build inputs without the product
+    library."""
+    deps = GEN_SRC + [HERE.parent / "prism-q_gb300" / "csrc" / "pq_host.h", HERE.parent / "include" / "prismq_md.h"]
+    if not force and GEN_LIB.exists() and all(GEN_LIB.stat().st_mtime >= d.stat().st_mtime for d in deps):
+        return GEN_LIB
+    BUILD.mkdir(exist_ok=True)
+    tmp = GEN_LIB.with_suffix(".so.tmp")
+    cmd = ["g++", *GEN_FLAGS, "-o", str(tmp), *map(str, GEN_SRC)]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"oracle generator build failed:\n{res.stderr}")
+    os.replace(tmp, GEN_LIB)
+    return GEN_LIB
+
+
+_gen = None
+
+
+def polyala(n_chains: int, n_residues: int, seed: int, density: float = 0.0, box_edge: float = 0.0,
+            compact: bool = True, stats: dict | None = None):
+    """A synthetic system from the oracle's build of the generator: the same
+    bits as the library's Topology.polyala / polyala_compact for the same
+    arguments.  Returns the package's Topology (a numpy container)."""
+    global _gen
+    import importlib
+
+    if _gen is None:
+        G = ctypes.CDLL(str(build_gen()))
+        G.orcgen_polyala.restype = ctypes.c_void_p
+        G.orcgen_polyala.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong, ctypes.c_double,
+                                     ctypes.c_double, ctypes.c_int, ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int]
+        G.orcgen_view.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        G.orcgen_free.argtypes = [ctypes.c_void_p]
+        _gen = G
+    pkg = importlib.import_module("prism-q_gb300")
+    st = (ctypes.c_double * 4)()
+    err = ctypes.create_string_buffer(256)
+    if not compact and not (density > 0.0):
+        density = 0.03
+    h = _gen.orcgen_polyala(n_chains, n_residues, seed, float(np.float32(density)), float(np.float32(box_edge)),
+                            1 if compact else 0, st, err, 256)
+    if not h:
+        raise RuntimeError(err.value.decode())
+    try:
+        t = pkg.TopologyStruct()
+        _gen.orcgen_view(h, ctypes.byref(t))
+        topo = pkg.Topology.from_struct(t)
+    finally:
+        _gen.orcgen_free(h)
+    if stats is not None:
+        stats.update(iterations=int(st[0]), max_overlap=st[1], max_outside=st[2], min_nonbonded=st[3])
+    return topo
 
 
 class OrcParams(ctypes.Structure):

@@ -280,19 +280,40 @@ long orc_pairs_ref27(int n, const float* pos, const float* grid_pos, float r2max
 
 long orc_pairs_brute(int n, const float* pos, float r2max, const int32_t* excl_off, const int32_t* excl,
                      int32_t* out, long cap) {
-  long total = 0;
-  for (int i = 0; i < n; ++i)
+  /* rows counted in parallel, then written at their prefix offsets: the
+   * output is the sequential (i, then j) order */
+  long* cnt = (long*)calloc((size_t)n + 1, sizeof(long));
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int i = 0; i < n; ++i) {
+    long c = 0;
     for (int j = i + 1; j < n; ++j) {
       const float r2 = r2_plain(pos[3 * j] - pos[3 * i], pos[3 * j + 1] - pos[3 * i + 1],
                                 pos[3 * j + 2] - pos[3 * i + 2]);
       if (r2 > r2max) continue;
       if (excluded(i, j, excl_off, excl)) continue;
-      if (total < cap && out) {
-        out[2 * total] = i;
-        out[2 * total + 1] = j;
-      }
-      ++total;
+      ++c;
     }
+    cnt[i + 1] = c;
+  }
+  for (int i = 0; i < n; ++i) cnt[i + 1] += cnt[i];
+  const long total = cnt[n];
+  if (out) {
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int i = 0; i < n; ++i) {
+      long k = cnt[i];
+      if (k >= cap) continue;
+      for (int j = i + 1; j < n && k < cap; ++j) {
+        const float r2 = r2_plain(pos[3 * j] - pos[3 * i], pos[3 * j + 1] - pos[3 * i + 1],
+                                  pos[3 * j + 2] - pos[3 * i + 2]);
+        if (r2 > r2max) continue;
+        if (excluded(i, j, excl_off, excl)) continue;
+        out[2 * k] = i;
+        out[2 * k + 1] = j;
+        ++k;
+      }
+    }
+  }
+  free(cnt);
   return total;
 }
 

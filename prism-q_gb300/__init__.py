@@ -158,6 +158,9 @@ def load() -> ctypes.CDLL:
         "prismq_abi_version": (I, []),
         "prismq_device_count": (I, []),
         "prismq_kernel_launches": (ctypes.c_longlong, []),
+        "prismq_set_device": (I, [ctypes.c_int32]),
+        "prismq_device_ordinal": (ctypes.c_int32, []),
+        "prismq_device_info": (I, [P]),
         "prismq_params_default": (None, [P]),
         "prismq_polyala_build": (I, [ctypes.c_int32, ctypes.c_int32, ctypes.c_uint64, ctypes.c_float,
                                      ctypes.c_float, P]),
@@ -264,6 +267,24 @@ def device_count() -> int:
 
 def kernel_launches() -> int:
     return int(load().prismq_kernel_launches())
+
+
+def set_device(ordinal: int) -> None:
+    """Select the library's CUDA device for the calling thread (its runtime is
+    its own: torch.cuda.set_device does not reach it)."""
+    _check(load().prismq_set_device(int(ordinal)))
+
+
+def device_ordinal() -> int:
+    """The library's current device on the calling thread (-1 without one)."""
+    return int(load().prismq_device_ordinal())
+
+
+def device_info() -> dict:
+    """{ordinal, sms, sm_clock_khz} of the library's current device."""
+    out = (ctypes.c_int32 * 3)()
+    _check(load().prismq_device_info(out))
+    return {"ordinal": int(out[0]), "sms": int(out[1]), "sm_clock_khz": int(out[2])}
 
 
 def debug_noise(seed: int, stream: int, atom: int, step: int, purpose: int) -> np.ndarray:
@@ -381,6 +402,11 @@ class Topology:
         L = load()
         t = TopologyStruct()
         _check(L.prismq_topology_view(buf, ctypes.byref(t)))
+        return cls.from_struct(t)
+
+    @classmethod
+    def from_struct(cls, t: TopologyStruct) -> "Topology":
+        """Copy the arrays a prismq_topology points at."""
         n = t.n_atoms
 
         def arr(ptr, count, dtype, shape=None):

@@ -1597,6 +1597,43 @@ int prismq_device_count(void) {
 }
 long long prismq_kernel_launches(void) { return g_launches.load(); }
 
+prismq_status prismq_set_device(int32_t ordinal) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return fail(PRISMQ_E_NO_DEVICE, "no CUDA device visible");
+  }
+  if (ordinal < 0 || ordinal >= n) return fail(PRISMQ_E_INVALID, "device ordinal out of range");
+  const cudaError_t e = cudaSetDevice(ordinal);
+  if (e != cudaSuccess) return fail(PRISMQ_E_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+  return PRISMQ_OK;
+}
+
+int32_t prismq_device_ordinal(void) {
+  int n = 0, d = -1;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0 || cudaGetDevice(&d) != cudaSuccess) {
+    cudaGetLastError();
+    return -1;
+  }
+  return d;
+}
+
+prismq_status prismq_device_info(int32_t out[3]) {
+  if (!out) return fail(PRISMQ_E_INVALID, "out is NULL");
+  const int d = prismq_device_ordinal();
+  if (d < 0) return fail(PRISMQ_E_NO_DEVICE, "no CUDA device visible");
+  int sms = 0, khz = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d) != cudaSuccess ||
+      cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, d) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(PRISMQ_E_CUDA, "cudaDeviceGetAttribute failed");
+  }
+  out[0] = d;
+  out[1] = sms;
+  out[2] = khz;
+  return PRISMQ_OK;
+}
+
 void prismq_params_default(prismq_params* p) {
   if (!p) return;
   p->dt = 0.004f;

@@ -16,9 +16,13 @@
 // symbol — so the first call on each device looks up its device address with
 // cudaGetSymbolAddress while that device is current, and later calls reuse
 // it.  That first call therefore does set-up work and should come before any
-// stream capture.  All calls share the one array: the kernels clear what must
-// start at zero on every call, and calls that overlap on the GPU (two streams,
-// two host threads) race on it and must be serialised by the caller.
+// stream capture.  The cached address belongs to the device's current
+// context: after cudaDeviceReset (or any teardown of the primary context) the
+// module is loaded again and the cache is stale, so this entry point must not
+// be used across a device reset.  All calls share the one array: the kernels
+// clear what must start at zero on every call, and calls that overlap on the
+// GPU (two streams, two host threads) race on it and must be serialised by
+// the caller.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -86,7 +90,11 @@ __global__ void __launch_bounds__(1024) k_na_cells(int* scr, const float* xyz, i
       }
       lo[d] = a;
       ext[d] = fmaxf(b - a, 1.0e-3f);
-      const float q = ext[d] / (r * 0.50005f);
+      // Cells at least 0.5005 r wide, so the ±2 stencil reaches 1.001 r: the
+      // 1e-3 margin covers the float rounding of (x - lo) * inv, about
+      // nd * 1.2e-7 cells per atom.  Capping nd (here, or in the product
+      // loop below) only widens the cells.
+      const float q = ext[d] / (r * 0.5005f);
       nd[d] = q >= 1.0f ? (int)fminf(q, 1024.0f) : 1;
     }
     while ((long long)nd[0] * nd[1] * nd[2] > kNaMaxCells) {
@@ -119,17 +127,43 @@ __global__ void __launch_bounds__(1024) k_na_cells(int* scr, const float* xyz, i
     atomicAdd(&start[c + 1], 1);
   }
   __syncthreads();
-  if (tid == 0) {  // serial prefix: at most kNaMaxCells entries, set-up cost only
-    int run = 0;
-    for (int c = 0; c < ncell; ++c) {
-      const int v = start[c + 1];
-      if (v > kNaCellCap) hdr[0] |= kNaErrCell;
-      cursor[c] = run;
-      run += v;
-      start[c + 1] = run;
+  // exclusive prefix of the cell counts, 1024 cells per pass (warp scans plus
+  // a carry), run on every call
+  {
+    __shared__ int wsum[32];
+    __shared__ int carry;
+    if (tid == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < ncell; base += 1024) {
+      const int c = base + tid;
+      const int v = c < ncell ? start[c + 1] : 0;
+      if (v > kNaCellCap) atomicOr(&hdr[0], kNaErrCell);
+      int x = v;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+      }
+      if (lane == 31) wsum[warp] = x;
+      __syncthreads();
+      if (warp == 0) {
+        int w = wsum[lane];
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(0xffffffffu, w, o);
+          if (lane >= o) w += y;
+        }
+        wsum[lane] = w;
+      }
+      __syncthreads();
+      const int incl = x + (warp > 0 ? wsum[warp - 1] : 0) + carry;
+      if (c < ncell) {
+        start[c + 1] = incl;
+        cursor[c] = incl - v;
+      }
+      __syncthreads();
+      if (tid == 1023) carry = incl;
+      __syncthreads();
     }
   }
-  __syncthreads();
   if (hdr[0]) return;
   for (int i = tid; i < n; i += 1024) catoms[atomicAdd(&cursor[acell[i]], 1)] = i;
   __syncthreads();

@@ -60,3 +60,31 @@ def test_stratified_sample(n, k):
 
     s = bench.stratified(n, k)
     assert s[0] == 0 and s[-1] == n - 1 and len(s) == min(n, k)
+
+
+def test_spawn_path_starts_one_rank_per_device(tmp_path):
+    """bench.py --gpus 2 without a launcher re-executes itself through
+    torch.distributed.run: two ranks, each selecting the library device of its
+    LOCAL_RANK, sharding the systems and reducing over gloo."""
+    import json
+
+    import bench
+    from conftest import ROOT
+
+    rc = bench.spawn_ranks(2, [str(ROOT / "tests" / "dist_rank.py"), str(tmp_path), "2"])
+    assert rc == 0
+    recs = sorted((json.loads((tmp_path / f"rank{r}.json").read_text()) for r in range(2)), key=lambda d: d["rank"])
+    assert [d["world"] for d in recs] == [2, 2]
+    assert [d["device"] for d in recs] == [d["local"] for d in recs] == [0, 1]
+    m0, m1 = recs[0]["mine"], recs[1]["mine"]
+    assert set(m0).isdisjoint(m1) and sorted(m0 + m1) == list(range(256))
+    assert recs[0]["t_max"] == recs[1]["t_max"] == 2.0
+    assert recs[0]["total"] == recs[1]["total"] == float(recs[0]["atoms"] + recs[1]["atoms"])
+
+
+def test_world_size_must_match_the_requested_gpus(monkeypatch):
+    import bench
+
+    monkeypatch.setenv("WORLD_SIZE", "1")
+    with pytest.raises(SystemExit):
+        bench.dist_setup(2)

@@ -115,3 +115,19 @@ def test_coulomb_constant_units():
     e, eps0, na = 1.602176634e-19, 8.8541878128e-12, 6.02214076e23
     k = e * e / (4 * math.pi * eps0) * 1e10 * na / 4184.0
     assert abs(k - 332.0636) / 332.0636 < 1e-5
+
+
+def test_oracle_generator_builds_the_library_systems(pq):
+    """The CPU legs of the benchmark build their inputs with the oracle's own
+    build of the generator; it yields the library's systems bit for bit."""
+    from oracle import oracle as orc
+
+    for args, kw in [((1, 120, 9), {}), ((3, 30, 4), {"box_edge": 25.0})]:
+        a = pq.Topology.polyala_compact(*args[:2], seed=args[2], **kw)
+        b = orc.polyala(*args, **kw)
+        for f in ("positions", "masses", "charges", "bonds", "angles", "dihedrals", "exceptions", "exclusions",
+                  "clusters"):
+            assert np.array_equal(getattr(a, f), getattr(b, f)), f
+    a = pq.Topology.polyala(1, 30, seed=3)
+    b = orc.polyala(1, 30, 3, compact=False)
+    assert np.array_equal(a.positions, b.positions)

@@ -38,7 +38,7 @@ def _rows_to_pairs(rows: np.ndarray, counts: np.ndarray) -> np.ndarray:
     return np.array(sorted(out), dtype=np.int32).reshape(-1, 2)
 
 
-def _run(pq, fn, pos: np.ndarray, row_cap: int = 1024):
+def _run(pq, fn, pos: np.ndarray, row_cap: int = 1024, expect: int = 0):
     import torch
 
     n = len(pos)
@@ -47,8 +47,15 @@ def _run(pq, fn, pos: np.ndarray, row_cap: int = 1024):
     d_cnt = torch.full((n,), -7, dtype=torch.int32, device="cuda")
     torch.cuda.synchronize()
     rc = fn(d_xyz.data_ptr(), n, 12.0, row_cap, d_rows.data_ptr(), d_cnt.data_ptr(), None)
-    assert rc == 0, pq.load().prismq_last_error()
+    assert rc == expect, (rc, pq.load().prismq_last_error())
     return d_rows.cpu().numpy(), d_cnt.cpu().numpy()
+
+
+def _existing_pairs(pq, pos: np.ndarray) -> np.ndarray:
+    eng = pq.NhsAmberFusedEngine(pq.Topology.point_cloud(pos), pq.Params())
+    want = eng.build_neighbors(pq.NLIST_COMPLETE)
+    eng.close()
+    return want
 
 
 def test_noalloc_rows_equal_existing_entry_point_twice(gpu, golden):
@@ -69,3 +76,44 @@ def test_noalloc_rejects_sizes_beyond_its_limits(gpu):
     fn = _noalloc(gpu)
     assert fn(None, 70000, 12.0, 64, None, None, None) == 4  # PRISMQ_E_CAPACITY
     assert fn(None, 100, 12.0, 2048, None, None, None) == 4
+
+
+def test_noalloc_long_thin_cloud_matches_brute_force(gpu, orc):
+    """A cloud 6,500 Å long (the grid caps at 1,024 cells on that axis, which
+    widens its cells) against the oracle's all-pairs enumeration."""
+    rng = np.random.default_rng(77)
+    n = 3000
+    pos = np.stack([rng.uniform(0.0, 6500.0, n), rng.uniform(0.0, 4.0, n), rng.uniform(0.0, 4.0, n)], axis=1)
+    pos = pos.astype(np.float32)
+    fn = _noalloc(gpu)
+    rows, cnt = _run(gpu, fn, pos)
+    got = _rows_to_pairs(rows, cnt)
+    want = orc.pairs_brute(pos, 144.0)
+    assert len(want) > 1000
+    assert np.array_equal(got, want)
+
+
+def test_noalloc_reports_overflows_and_recovers(gpu, golden):
+    """A row longer than row_cap and a cell of more than 512 atoms are reported
+    with their status and -1 counts; the next ordinary call through the same
+    scratch again equals the existing entry point."""
+    fn = _noalloc(gpu)
+    cloud = golden["cloud_2000/pos"]
+    want = _existing_pairs(gpu, cloud)
+    deg = np.bincount(want.reshape(-1), minlength=len(cloud))
+    # rows capped at the median row length: the longer rows overflow, the others are whole
+    cap = int(np.median(deg))
+    rows, cnt = _run(gpu, fn, cloud, row_cap=cap, expect=6)  # PRISMQ_E_NEIGHBOR_OVERFLOW
+    assert np.array_equal(cnt == -1, deg > cap)
+    assert (deg <= cap).any() and (deg > cap).any()
+    for i in np.nonzero(deg <= cap)[0]:
+        part = sorted(set(want[want[:, 0] == i, 1]) | set(want[want[:, 1] == i, 0]))
+        assert sorted(rows[i, :cnt[i]].tolist()) == part
+    # 600 atoms inside one cell
+    rng = np.random.default_rng(5)
+    dense = rng.uniform(0.0, 1.0, size=(600, 3)).astype(np.float32)
+    _, cnt = _run(gpu, fn, dense, expect=5)  # PRISMQ_E_CELL_OVERFLOW
+    assert (cnt == -1).all()
+    # an ordinary call afterwards
+    rows, cnt = _run(gpu, fn, cloud)
+    assert np.array_equal(_rows_to_pairs(rows, cnt), want)
