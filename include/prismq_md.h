@@ -42,7 +42,7 @@ typedef enum prismq_status {
   PRISMQ_E_NO_DEVICE = 3,        /* no CUDA device visible */
   PRISMQ_E_CAPACITY = 4,         /* caller buffer or arena too small */
   PRISMQ_E_CELL_OVERFLOW = 5,    /* a cell held more atoms than the grid allows */
-  PRISMQ_E_NEIGHBOR_OVERFLOW = 6,/* an atom had more neighbours than the row holds */
+  PRISMQ_E_NEIGHBOR_OVERFLOW = 6,/* an atom's row or a cluster's tile list was full */
   PRISMQ_E_SHAKE = 7,            /* SHAKE did not converge in max_iter */
   PRISMQ_E_RATTLE = 8,           /* RATTLE did not converge in max_iter */
   PRISMQ_E_NONFINITE = 9,        /* NaN/Inf in state or forces */
@@ -415,6 +415,20 @@ prismq_status prismq_batch_frames_configure(prismq_batch* b, int32_t slot, int32
                                             int32_t with_velocities);
 prismq_status prismq_batch_frames_read(prismq_batch* b, int32_t slot, float* xyz, float* vxyz, int64_t* steps,
                                        int32_t max_frames, int32_t* n_out, int64_t* dropped);
+/* Layout of the production neighbour list (FP32 systems in complete mode):
+ *   1 (default) cluster-pair tiles: i-clusters of 8 consecutive atoms against
+ *     j-clusters of 4, one {j-cluster, 32-bit pair mask} per tile, the tiles
+ *     of an i-cluster in ascending j-cluster order (at most 768);
+ *   0 one row of partner indices per atom (at most 1024), the layout REF27
+ *     and FP64 runs always use.
+ * The pair set is the same; the forces differ only in the grouping of their
+ * FP32 partial sums, and each layout is bit-reproducible on its own.  Setting
+ * it rebuilds every resident system's list before the next step, so set it
+ * before stepping.  No counterpart in the reference, which keeps one full
+ * row per atom (nhs_neighbor_warp.cuh:10-121). */
+prismq_status prismq_batch_set_pair_layout(prismq_batch* b, int32_t layout);
+int32_t prismq_batch_pair_layout(const prismq_batch* b);
+prismq_status prismq_set_pair_layout(prismq_system* sys, int32_t layout);
 /* The autotuner's choice for the batch's force kernel: out[0] = variant
  * (-1 before the first step), out[1] = threads per block, out[2] = minimum
  * resident blocks per SM given to the register allocator.  The launch shape

@@ -128,6 +128,8 @@ def lib() -> ctypes.CDLL:
         L.orc_shake_all.argtypes = [P, P]
         L.orc_kick_all.argtypes = [P, P]
         L.orc_clamp_all.argtypes = [P]
+        L.orc_ou_all.argtypes = [P, P, ctypes.c_float]
+        L.orc_ou_all.restype = None
         L.orc_term_forces.argtypes = [P, P, P, P]
         L.orc_phases.argtypes = [P, ctypes.c_int, P, ctypes.c_longlong]
         L.orc_com_remove.argtypes = [P]
@@ -283,6 +285,11 @@ class OracleSystem:
 
     def clamp_all(self) -> None:
         lib().orc_clamp_all(self.h)
+
+    def ou_all(self, z, c1: float) -> None:
+        """One OU half-step of every atom with the given normals [n, 3] and c1."""
+        za = np.ascontiguousarray(z, dtype=np.float32).reshape(-1)
+        lib().orc_ou_all(self.h, _ptr(za), float(c1))
 
     def term_forces(self, nb: int, na: int, nd: int):
         fb = np.zeros((nb, 2, 3), np.float32)

@@ -1169,6 +1169,16 @@ void orc_clamp_all(orc_sys* s) {
   for (int a = 0; a < s->n; ++a) clamp_atom(s, a);
 }
 
+/* One OU half-step of every atom with given normals z[3n] and a given c1,
+ * the arithmetic of ou_atom (langevin_thermostat, nhs_amber_fused.cu:1713-1744). */
+void orc_ou_all(orc_sys* s, const float* z, float c1) {
+  if (s->p.gamma == 0.0f) return;
+  for (int a = 0; a < s->n; ++a) {
+    const float c2 = sqrtf((1.0f - c1 * c1) * ORC_AKMA * ORC_KB * s->p.temperature / s->m[a]);
+    for (int d = 0; d < 3; ++d) s->v[3 * a + d] = c1 * s->v[3 * a + d] + c2 * z[3 * a + d];
+  }
+}
+
 /* bonds -> fb[nb][2][3], angles -> fa[na][3][3], torsion terms -> fd[nd][4][3] */
 void orc_term_forces(const orc_sys* s, float* fb, float* fa, float* fd) {
   for (int t = 0; t < s->nb; ++t) {

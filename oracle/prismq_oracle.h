@@ -74,6 +74,7 @@ int orc_rattle_all(orc_sys* s);
 int orc_shake_all(orc_sys* s, const float* xs);
 void orc_kick_all(orc_sys* s, const float* f);
 void orc_clamp_all(orc_sys* s);
+void orc_ou_all(orc_sys* s, const float* z, float c1);
 void orc_term_forces(const orc_sys* s, float* fb, float* fa, float* fd);
 
 /* Integrator phase sets on the current state with forces given as int64

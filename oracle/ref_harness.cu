@@ -12,6 +12,8 @@
 //   compute_nonbonded_force       :644 (ordinary pairs and exact exceptions)
 //   apply_force_half_kick_with_intervention_work  :1750
 //   apply_exact_force_half_kick   :1792
+//   langevin_thermostat           :1713 (the OU half-step of phases
+//                                 OU_HALF_N / OU_HALF_NP1, :3656-3666)
 //   shake_cluster_positions       :1890
 //   rattle_cluster_velocities     :2176
 // and the reference's nhs_velocity_safety_clamp kernel (:11148) is launched
@@ -135,4 +137,28 @@ extern "C" __global__ void refh_protocol_init(ProtocolState* p, float temperatur
   unsigned char* b = reinterpret_cast<unsigned char*>(p);
   for (int k = 0; k < (int)sizeof(ProtocolState); ++k) b[k] = 0;
   p->current_temperature = temperature;
+}
+
+// OU half-step of atom a by the reference's own thermostat, as the OU phases
+// call it (langevin_thermostat with 0.5 dt, nhs_amber_fused.cu:3656-3666),
+// from a cuRAND state initialised as init_rng_states does
+// (curand_init(seed, a, 0), :11308).  The three normals the thermostat
+// draws are recorded from a copy of that state, and c1 is evaluated as the
+// thermostat evaluates it, so a restatement given the same normals and c1
+// can be compared bit for bit.
+extern "C" __global__ void refh_ou(int n, float3* vel, const float* mass, float temperature, float gamma, float dt,
+                                   unsigned long long seed, float* normals, float* c1_out) {
+  const int a = tid1();
+  if (a >= n) return;
+  curandState st;
+  curand_init(seed, a, 0, &st);
+  curandState cp = st;
+  normals[3 * a] = curand_normal(&cp);
+  normals[3 * a + 1] = curand_normal(&cp);
+  normals[3 * a + 2] = curand_normal(&cp);
+  const float dt_half = 0.5f * dt;
+  float3 v = vel[a];
+  langevin_thermostat(v, mass[a], temperature, gamma, dt_half, &st, nullptr);
+  vel[a] = v;
+  if (a == 0) c1_out[0] = expf(-gamma * dt_half);
 }

@@ -263,3 +263,21 @@ def clamp(v, mass, temperature, nofma=True):
         return D.get(d_v, vv)
     finally:
         D.free()
+
+
+def ou(v, mass, temperature, gamma, dt, seed, nofma=True):
+    """One OU half-step by the reference's langevin_thermostat from cuRAND
+    states initialised as init_rng_states does; returns (v, normals [n, 3],
+    c1) with the normals the thermostat drew and its c1."""
+    D = _Dev()
+    try:
+        vv = _pos3(v)
+        n = len(vv)
+        z = np.zeros((n, 3), np.float32)
+        c1 = np.zeros(1, np.float32)
+        d_v, d_z, d_c1 = D.put(vv), D.put(z), D.put(c1)
+        D.launch(nofma, "refh_ou", n, [_i(n), d_v, D.put(np.asarray(mass, np.float32)), _f(temperature), _f(gamma),
+                                      _f(dt), ctypes.c_uint64(int(seed)), d_z, d_c1])
+        return D.get(d_v, vv), D.get(d_z, z), float(D.get(d_c1, c1)[0])
+    finally:
+        D.free()

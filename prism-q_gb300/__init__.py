@@ -30,6 +30,7 @@ STATUS = {
 NLIST_COMPLETE, NLIST_REF27 = 0, 1
 PRECISION_FP32, PRECISION_FP64 = 0, 1
 PHASES_PRE, PHASES_POST = 1, 2
+PAIR_ROWS, PAIR_TILES = 0, 1
 
 
 class PrismQError(RuntimeError):
@@ -159,6 +160,9 @@ def load() -> ctypes.CDLL:
         "prismq_device_count": (I, []),
         "prismq_kernel_launches": (ctypes.c_longlong, []),
         "prismq_set_device": (I, [ctypes.c_int32]),
+        "prismq_batch_set_pair_layout": (I, [P, ctypes.c_int32]),
+        "prismq_batch_pair_layout": (ctypes.c_int32, [P]),
+        "prismq_set_pair_layout": (I, [P, ctypes.c_int32]),
         "prismq_device_ordinal": (ctypes.c_int32, []),
         "prismq_device_info": (I, [P]),
         "prismq_params_default": (None, [P]),
@@ -683,6 +687,10 @@ class NhsAmberFusedEngine:
     def rebuild_neighbor_lists(self) -> np.ndarray:
         return self.build_neighbors(NLIST_REF27)
 
+    def set_pair_layout(self, layout: int) -> None:
+        """PAIR_TILES (default) or PAIR_ROWS for the production list; set before stepping."""
+        _check(load().prismq_set_pair_layout(self.h, int(layout)))
+
     def debug_phases(self, which: int, step: int) -> None:
         _check(load().prismq_debug_phases(self.h, which, step))
 
@@ -814,6 +822,14 @@ class Batch:
                 raise ValueError(f"state arrays must be contiguous float32 of {n} values")
         _check(load().prismq_batch_step_host(self.h, int(n_steps), _ptr(xyz_in), _ptr(vxyz_in), _ptr(xyz_out),
                                              _ptr(vxyz_out)))
+
+    def set_pair_layout(self, layout: int) -> None:
+        """PAIR_TILES (default) or PAIR_ROWS for the production list; set before stepping."""
+        _check(load().prismq_batch_set_pair_layout(self.h, int(layout)))
+
+    @property
+    def pair_layout(self) -> int:
+        return int(load().prismq_batch_pair_layout(self.h))
 
     def set_force_variant(self, variant: int) -> int:
         """Pin the force kernel's launch shape (-1: autotune); returns the number of shapes."""

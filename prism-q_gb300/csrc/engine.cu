@@ -776,7 +776,7 @@ struct prismq_batch {
     if (gexec_tail) cudaGraphExecDestroy(gexec_tail);
     void* ptrs[] = {A.pos, A.vel, A.lj, A.xref, A.f, A.pe, A.atom_sys, A.mask_all, A.mask_ref, A.far,
                     A.far_list, A.inc, A.inc_list, A.ex_idx, A.ex_partner, A.ex_par, A.exc, A.grp, A.grp_refs, A.bonds, A.angles,
-                    A.dihs, A.units, A.unit_order, A.noise, A.nbr, A.nnbr, A.cell_start, A.cell_atoms, A.atom_cell, A.work, A.work_ctl, A.big_list, A.sys,
+                    A.dihs, A.units, A.unit_order, A.noise, A.nbr, A.nnbr, A.tiles, A.ntile, A.cell_start, A.cell_atoms, A.atom_cell, A.work, A.work_ctl, A.big_list, A.sys,
                     A.pos64, A.vel64, A.f64, A.lj64, d_energy, d_stage, d_stage2, d_stage64};
     for (void* p : ptrs)
       if (p) cudaFree(p);
@@ -1027,7 +1027,9 @@ struct prismq_batch {
     if (stt & kStShake) return fail(PRISMQ_E_SHAKE, "SHAKE did not converge" + where);
     if (stt & kStRattle) return fail(PRISMQ_E_RATTLE, "RATTLE did not converge" + where);
     if (stt & kStCellOverflow) return fail(PRISMQ_E_CELL_OVERFLOW, "cell occupancy above 512" + where);
-    if (stt & kStNbrOverflow) return fail(PRISMQ_E_NEIGHBOR_OVERFLOW, "neighbour row above 1024" + where);
+    if (stt & kStNbrOverflow)
+      return fail(PRISMQ_E_NEIGHBOR_OVERFLOW,
+                  "neighbour list above capacity (a row above 1024, or above 768 tiles per 8-atom cluster)" + where);
     return fail(PRISMQ_E_NONFINITE, "non-finite state" + where);
   }
 
@@ -1253,6 +1255,8 @@ prismq_status batch_alloc(prismq_batch* B, int64_t atom_cap, int sys_cap, int64_
   PQ_ALLOC(A.noise, 2 * atom_cap);
   PQ_ALLOC(A.nbr, (atom_cap / 32) * (int64_t)kNbrCap * 32);
   PQ_ALLOC(A.nnbr, atom_cap);
+  PQ_ALLOC(A.tiles, (atom_cap / 8) * (int64_t)kTileCap);
+  PQ_ALLOC(A.ntile, atom_cap / 8 + 1);
   PQ_ALLOC(A.cell_start, A.cell_cap);
   PQ_ALLOC(A.cell_atoms, atom_cap);
   PQ_ALLOC(A.atom_cell, atom_cap);
@@ -1277,6 +1281,7 @@ prismq_status batch_alloc(prismq_batch* B, int64_t atom_cap, int sys_cap, int64_
   if (A.fp64) PQ_CK(cudaMemsetAsync(A.f64, 0, sizeof(double) * 3 * atom_cap, B->st));
   PQ_CK(cudaMemsetAsync(A.sys, 0, sizeof(SysDev) * sys_cap, B->st));
   PQ_CK(cudaMemsetAsync(A.nnbr, 0, sizeof(int) * atom_cap, B->st));
+  PQ_CK(cudaMemsetAsync(A.ntile, 0, sizeof(int) * (atom_cap / 8 + 1), B->st));
   PQ_CK(cudaMemsetAsync(A.grp, 0, sizeof(int2) * (atom_cap / kForceGroup + 1), B->st));
   PQ_CK(cudaMemsetAsync(A.work_ctl, 0, sizeof(int) * 4, B->st));
   PQ_CK(cudaMemsetAsync(A.f, 0, sizeof(long long) * 3 * atom_cap, B->st));
@@ -1454,6 +1459,7 @@ prismq_status batch_admit(prismq_batch* B, const Lowered& L0, const prismq_param
     PQ_CK(cudaStreamSynchronize(st));  // the host staging vectors die here
   }
   PQ_CK(cudaMemsetAsync(A.nnbr + ab, 0, sizeof(int) * L.n, st));
+  PQ_CK(cudaMemsetAsync(A.ntile + ab / 8, 0, sizeof(int) * ((L.n + 7) / 8), st));
   PQ_CK(cudaMemsetAsync(A.f + ab, 0, sizeof(long long) * L.n, st));
   PQ_CK(cudaMemsetAsync(A.f + A.atom_cap + ab, 0, sizeof(long long) * L.n, st));
   PQ_CK(cudaMemsetAsync(A.f + 2 * A.atom_cap + ab, 0, sizeof(long long) * L.n, st));
@@ -1780,6 +1786,27 @@ prismq_status prismq_batch_set_force_variant(prismq_batch* b, int32_t variant, i
   b->force_variant = variant;
   b->tuned_span = 0;
   return PRISMQ_OK;
+}
+
+prismq_status prismq_batch_set_pair_layout(prismq_batch* b, int32_t layout) {
+  if (!b) return fail(PRISMQ_E_INVALID, "batch is NULL");
+  if (layout != 0 && layout != 1) return fail(PRISMQ_E_INVALID, "pair layout must be 0 (rows) or 1 (tiles)");
+  if (layout == b->A.pair_layout) return PRISMQ_OK;
+  b->A.pair_layout = layout;
+  b->graph_dirty = true;
+  for (int s = 0; s < (int)b->slots.size(); ++s) {
+    if (!b->slots[s].active) continue;
+    const prismq_status rc = mark_prime(b, s);
+    if (rc != PRISMQ_OK) return rc;
+  }
+  return PRISMQ_OK;
+}
+
+int32_t prismq_batch_pair_layout(const prismq_batch* b) { return b ? b->A.pair_layout : -1; }
+
+prismq_status prismq_set_pair_layout(prismq_system* sys, int32_t layout) {
+  if (!sys) return fail(PRISMQ_E_INVALID, "system is NULL");
+  return prismq_batch_set_pair_layout(sys->b, layout);
 }
 
 prismq_status prismq_batch_tuning(prismq_batch* b, int32_t out[3]) {
@@ -2238,12 +2265,26 @@ prismq_status prismq_build_neighbors(prismq_system* sys, prismq_nlist_mode mode,
   g_launches += 3 + (B->max_big_atoms > 0 ? 4 : 0);
   PQ_CK(cudaGetLastError());
   const int64_t n = R.n_atoms, ab = R.atom_b;
-  std::vector<int> cnt(n);
-  PQ_CK(cudaMemcpyAsync(cnt.data(), B->A.nnbr + ab, sizeof(int) * n, cudaMemcpyDeviceToHost, B->st));
   const int64_t g0 = ab / 8, g1 = (ab + n + 7) / 8;
-  std::vector<int> rows((size_t)(g1 - g0) * kNbrCap * 8);
-  PQ_CK(cudaMemcpyAsync(rows.data(), B->A.nbr + g0 * kNbrCap * 8, sizeof(int) * rows.size(),
-                        cudaMemcpyDeviceToHost, B->st));
+  SysDev probe{};
+  probe.nbr_mode = mode == PRISMQ_NLIST_REF27 ? 1 : 0;
+  const bool tiles = uses_tiles(B->A, probe);
+  std::vector<int> cnt, rows, ntile;
+  std::vector<int2> tl;
+  if (tiles) {
+    ntile.resize(g1 - g0);
+    tl.resize((size_t)(g1 - g0) * kTileCap);
+    PQ_CK(cudaMemcpyAsync(ntile.data(), B->A.ntile + g0, sizeof(int) * ntile.size(), cudaMemcpyDeviceToHost,
+                          B->st));
+    PQ_CK(cudaMemcpyAsync(tl.data(), B->A.tiles + g0 * kTileCap, sizeof(int2) * tl.size(), cudaMemcpyDeviceToHost,
+                          B->st));
+  } else {
+    cnt.resize(n);
+    rows.resize((size_t)(g1 - g0) * kNbrCap * 8);
+    PQ_CK(cudaMemcpyAsync(cnt.data(), B->A.nnbr + ab, sizeof(int) * n, cudaMemcpyDeviceToHost, B->st));
+    PQ_CK(cudaMemcpyAsync(rows.data(), B->A.nbr + g0 * kNbrCap * 8, sizeof(int) * rows.size(),
+                          cudaMemcpyDeviceToHost, B->st));
+  }
   PQ_CK(cudaStreamSynchronize(B->st));
   prismq_status st = B->check_status(sys->slot);
   // restore the production list
@@ -2255,11 +2296,24 @@ prismq_status prismq_build_neighbors(prismq_system* sys, prismq_nlist_mode mode,
   PQ_CK(cudaStreamSynchronize(B->st));
   if (st != PRISMQ_OK) return st;
   std::vector<std::pair<int, int>> pairs;
-  for (int64_t i = 0; i < n; ++i) {
-    const int64_t a = ab + i;
-    for (int k = 0; k < cnt[i]; ++k) {
-      const int j = rows[nbr_index(a, k) - g0 * kNbrCap * 8] - (int)ab;
-      if (j > i) pairs.emplace_back((int)i, j);
+  if (tiles) {
+    // every set bit of a tile is one pair of the list (both orders appear)
+    for (int64_t g = g0; g < g1; ++g)
+      for (int t = 0; t < ntile[g - g0]; ++t) {
+        const int2 e = tl[(size_t)(g - g0) * kTileCap + t];
+        for (int bit = 0; bit < 32; ++bit) {
+          if (!(((unsigned)e.y >> bit) & 1u)) continue;
+          const int i = (int)(8 * g + (bit & 7) - ab), j = 4 * e.x + (bit >> 3) - (int)ab;
+          if (j > i) pairs.emplace_back(i, j);
+        }
+      }
+  } else {
+    for (int64_t i = 0; i < n; ++i) {
+      const int64_t a = ab + i;
+      for (int k = 0; k < cnt[i]; ++k) {
+        const int j = rows[nbr_index(a, k) - g0 * kNbrCap * 8] - (int)ab;
+        if (j > i) pairs.emplace_back((int)i, j);
+      }
     }
   }
   std::sort(pairs.begin(), pairs.end());

@@ -384,6 +384,137 @@ __device__ __forceinline__ bool exception_out(const R4<R>* pos, const ExcT e, Te
   return true;
 }
 
+// Ordinary pairs from cluster-pair tiles (FP32 complete-mode systems).  Warp
+// w of the block owns i-cluster w (atoms a0 + 8w .. a0 + 8w + 7) and lane
+// i + 8 jj evaluates pair (i, jj) of every tile in the i-cluster's list, so a
+// tile's four j atoms are read once for all eight i atoms (a 64-byte line
+// shared by the warp) and the list costs 8 bytes per 32 pair slots.  A
+// tile whose pairs all lie outside the cutoff costs only the distance test
+// (warp vote).  The inclusion test (list bit, r^2 in [0.01, cutoff^2)) and
+// the pair law are the row path's; lane jj sums FP32 over its pairs of 32
+// consecutive tiles, then accumulates in int64, and an atom's four lanes are
+// summed exactly, so the force depends only on the system's own tile list.
+template <bool kEnergy>
+__device__ __forceinline__ void force_tiles(const Arena& A, int64_t n_span, int s0, const SysDev* Sp, int64_t a0,
+                                            int tid, const float* slot_x, const float* slot_y, const float* slot_z,
+                                            const double* slot_e, const int* s_base, const int* s_nb,
+                                            const int* s_na, const int* s_nd) {
+  const int lane = tid & 31, w = tid >> 5;
+  const int64_t c0 = a0 + (w << 3);  // the warp's i-cluster
+  if (c0 >= n_span || A.atom_sys[c0] != s0) return;  // whole warp
+  const int ga = (w << 3) + (lane & 7), q = lane >> 3;
+  const int64_t a64 = a0 + ga;
+  const bool mine = a64 < n_span && A.atom_sys[a64] == s0;
+  const int a = mine ? (int)a64 : (int)c0;  // lanes past the system's end stand in with the cluster's first atom
+  const float cut2 = Sp->cut2;
+  Acc<float> f{};
+  double eb = 0.0, ea = 0.0, ed = 0.0, ex = 0.0, en = 0.0;
+  if (mine) {
+    const int base = s_base[ga], nb = s_nb[ga], na = s_na[ga], nd = s_nd[ga];
+    for (int t = q; t < nb; t += kLanes) {
+      f.x += slot_x[base + t];
+      f.y += slot_y[base + t];
+      f.z += slot_z[base + t];
+      if (kEnergy) eb += slot_e[base + t];
+    }
+    for (int t = q; t < na; t += kLanes) {
+      const int sl = base + nb + t;
+      f.x += slot_x[sl];
+      f.y += slot_y[sl];
+      f.z += slot_z[sl];
+      if (kEnergy) ea += slot_e[sl];
+    }
+    for (int t = q; t < nd; t += kLanes) {
+      const int sl = base + nb + na + t;
+      f.x += slot_x[sl];
+      f.y += slot_y[sl];
+      f.z += slot_z[sl];
+      if (kEnergy) ed += slot_e[sl];
+    }
+    f.flush();
+    const int ne = A.ex_idx[a].y;
+    for (int t = q; t < ne; t += kLanes) {
+      const int sl = base + nb + na + nd + t;
+      f.x += slot_x[sl];
+      f.y += slot_y[sl];
+      f.z += slot_z[sl];
+      if (kEnergy) ex += slot_e[sl];
+    }
+    f.flush();
+  }
+  const float4 pi = A.pos[a];
+  const float2 li = A.lj[a];
+  const float qi = pi.w;
+  const int64_t g = c0 >> 3;
+  const int nt = A.ntile[g];
+  const int2* tl = A.tiles + g * kTileCap;
+  const unsigned lanebit = 1u << lane;
+  float inv_rc = 0.0f;
+  if (kEnergy) inv_rc = rsqrtf(cut2);
+  for (int t0 = 0; t0 < nt; t0 += 32) {
+    const int2 e = t0 + lane < nt ? __ldg(tl + t0 + lane) : make_int2(0, 0);
+    const int m = min(32, nt - t0);
+    for (int u = 0; u < m; ++u) {
+      const int jc = __shfl_sync(0xffffffffu, e.x, u);
+      const unsigned bits = (unsigned)__shfl_sync(0xffffffffu, e.y, u);
+      const int j = (jc << 2) + q;
+      const float4 pj = __ldg(A.pos + j);
+      const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+      const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+      const bool in = (bits & lanebit) != 0u && r2 < cut2 && r2 >= kMinPairR2;
+      if (__any_sync(0xffffffffu, in)) {
+        const float2 lj = __ldg(A.lj + j);
+        const float sig = li.x + lj.x, eps = li.y * lj.y, qq = qi * pj.w;
+        float inv_r, s6;
+        float fs = pair_scalar<float>(fmaxf(r2, kMinPairR2), sig, eps, qq, inv_r, s6);
+        fs = in ? fs : 0.0f;
+        f.x -= fs * (in ? dx : 0.0f);
+        f.y -= fs * (in ? dy : 0.0f);
+        f.z -= fs * (in ? dz : 0.0f);
+        if (kEnergy && in) {
+          const float sc2 = sig * sig * inv_rc * inv_rc;
+          const float sc6 = sc2 * sc2 * sc2;
+          const double v = 4.0 * (double)eps * (((double)s6 * (double)s6 - (double)s6) -
+                                                ((double)sc6 * (double)sc6 - (double)sc6)) +
+                           (double)kCoulomb * (double)qq * ((double)inv_r - (double)inv_rc);
+          en += v * 0.5;
+        }
+      }
+    }
+    f.flush();
+  }
+  long long X = f.X, Y = f.Y, Z = f.Z;
+#pragma unroll
+  for (int o = 8; o <= 16; o <<= 1) {
+    X += __shfl_xor_sync(0xffffffffu, X, o);
+    Y += __shfl_xor_sync(0xffffffffu, Y, o);
+    Z += __shfl_xor_sync(0xffffffffu, Z, o);
+  }
+  if (kEnergy) {
+#pragma unroll
+    for (int o = 8; o <= 16; o <<= 1) {
+      eb += __shfl_xor_sync(0xffffffffu, eb, o);
+      ea += __shfl_xor_sync(0xffffffffu, ea, o);
+      ed += __shfl_xor_sync(0xffffffffu, ed, o);
+      ex += __shfl_xor_sync(0xffffffffu, ex, o);
+      en += __shfl_xor_sync(0xffffffffu, en, o);
+    }
+  }
+  if (mine && q == 0) {
+    const int64_t cap = A.atom_cap;
+    A.f[a] = X;
+    A.f[cap + a] = Y;
+    A.f[2 * cap + a] = Z;
+    if (kEnergy) {
+      A.pe[a] = eb;
+      A.pe[cap + a] = ea;
+      A.pe[2 * cap + a] = ed;
+      A.pe[3 * cap + a] = ex;
+      A.pe[4 * cap + a] = en;
+    }
+  }
+}
+
 // One force block = one 32-atom group, four lanes per atom.
 //   1. The block evaluates every bonded term and exception pair with a member
 //      in the group once (one thread per term), and drops each member's
@@ -494,6 +625,14 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_force(Arena A, int64_t n_sp
   }
   if (bad) atomicOr(&A.sys[s0].status, kStNonfinite);
   __syncthreads();
+  if constexpr (sizeof(R) == 4) {
+    if (uses_tiles(A, *Sp)) {
+      force_tiles<kEnergy>(A, n_span, s0, Sp, a0, tid, reinterpret_cast<const float*>(slot_x),
+                           reinterpret_cast<const float*>(slot_y), reinterpret_cast<const float*>(slot_z), slot_e,
+                           s_base, s_nb, s_na, s_nd);
+      return;
+    }
+  }
   const int ga = tid >> 2;  // the thread's atom within the group
   const int64_t a64 = a0 + ga;
   if (a64 >= n_span || A.atom_sys[a64] != s0) return;

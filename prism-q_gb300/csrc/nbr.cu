@@ -610,7 +610,140 @@ struct GroupShared {
   int2 far[8];
   int run_b[kMaxRuns];        // first sorted-atom index of the run
   int run_off[kMaxRuns + 1];  // exclusive prefix of run lengths
+  // cluster-pair tiles of the group: open-addressing table keyed by the
+  // system-local j-cluster + 1 (0 = empty), with the OR of its pair bits
+  int tkey[kTileHash];
+  unsigned tmask[kTileHash];
+  int tcount;  // keys in the table
 };
+
+// Add pair bits to j-cluster jc_local's entry of the group's tile table.  The
+// table's contents (a set of keys with OR-ed masks) do not depend on the order
+// of insertion.  Returns false once the group holds more than kTileCap
+// j-clusters (the table then stays at most 3/4 full, so probes stay short).
+__device__ __forceinline__ bool tile_insert(GroupShared& sh, int jc_local, unsigned bits) {
+  if (*(volatile int*)&sh.tcount > kTileCap) return false;
+  const int key = jc_local + 1;
+  unsigned h = ((unsigned)key * 2654435761u) >> 22;  // top 10 bits: kTileHash = 1024 slots
+  for (int probe = 0; probe < kTileHash; ++probe) {
+    const int prev = atomicCAS(&sh.tkey[h], 0, key);
+    if (prev == 0 || prev == key) {
+      atomicOr(&sh.tmask[h], bits);
+      return prev == key || atomicAdd(&sh.tcount, 1) < kTileCap;
+    }
+    h = (h + 1) & (kTileHash - 1);
+  }
+  return false;
+}
+
+// The group's tiles out of its table: compacted, sorted by j-cluster (so the
+// list order is a function of the pair set alone) and written as
+// {global j-cluster, mask}.  Returns the tile count, or -1 past kTileCap.
+__device__ int tile_flush(const Arena& A, GroupShared& sh, int64_t g, int ab, int lane) {
+  __syncwarp();
+  int cnt = 0;
+  for (int b = 0; b < kTileHash; b += 32) {
+    const int k = sh.tkey[b + lane];
+    const unsigned m = sh.tmask[b + lane];
+    const unsigned bal = __ballot_sync(0xffffffffu, k != 0);
+    __syncwarp();
+    if (k != 0) {
+      const int at = cnt + __popc(bal & ((1u << lane) - 1u));
+      sh.tkey[at] = k;
+      sh.tmask[at] = m;
+    }
+    cnt += __popc(bal);
+    __syncwarp();
+  }
+  if (cnt > kTileCap) return -1;
+  int p2 = 1;
+  while (p2 < cnt) p2 <<= 1;
+  for (int k = cnt + lane; k < p2; k += 32) sh.tkey[k] = 0x7fffffff;
+  __syncwarp();
+  for (int w = 2; w <= p2; w <<= 1)
+    for (int st = w >> 1; st > 0; st >>= 1) {
+      for (int k = lane; k < p2; k += 32) {
+        const int q = k ^ st;
+        if (q > k) {
+          const int x = sh.tkey[k], y = sh.tkey[q];
+          const bool up = (k & w) == 0;
+          if ((up && x > y) || (!up && x < y)) {
+            sh.tkey[k] = y;
+            sh.tkey[q] = x;
+            const unsigned mx = sh.tmask[k];
+            sh.tmask[k] = sh.tmask[q];
+            sh.tmask[q] = mx;
+          }
+        }
+      }
+      __syncwarp();
+    }
+  int2* out = A.tiles + g * kTileCap;
+  for (int k = lane; k < cnt; k += 32) out[k] = make_int2((ab >> 2) + sh.tkey[k] - 1, (int)sh.tmask[k]);
+  if (lane == 0) A.ntile[g] = cnt;
+  __syncwarp();
+  return cnt;
+}
+
+// Tiles input of one atom (i of the group) from its own stencil, as
+// build_row scans it: used for a group whose union stencil is too large.
+__device__ bool tile_atom(const Arena& A, const SysDev* Sp, GroupShared& sh, int a, int i, int lane) {
+  const int ab = Sp->atom_begin;
+  const int dims[3] = {Sp->g_dims[0], Sp->g_dims[1], Sp->g_dims[2]};
+  const float r2max = Sp->rlist2;
+  const int* start = A.cell_start + Sp->cell_begin;
+  const float4 pi = A.pos[a];
+  const int cell = A.atom_cell[a];
+  const int cx = cell % dims[0], cy = (cell / dims[0]) % dims[1], cz = cell / (dims[0] * dims[1]);
+  const unsigned long long mask = A.mask_all[a];
+  const int2 far = A.far[a];
+  const float lox = Sp->g_lo[0], loy = Sp->g_lo[1], loz = Sp->g_lo[2];
+  const float ivx = Sp->g_inv_edge[0];
+  const float ey = 1.0f / Sp->g_inv_edge[1], ez = 1.0f / Sp->g_inv_edge[2];
+  bool ok = true;
+  for (int dz = -2; dz <= 2; ++dz) {
+    const int z = cz + dz;
+    if (z < 0 || z >= dims[2]) continue;
+    for (int dy = -2; dy <= 2; ++dy) {
+      const int y = cy + dy;
+      if (y < 0 || y >= dims[1]) continue;
+      const float sy = fmaxf(0.0f, fmaxf((loy + (float)y * ey) - pi.y, pi.y - (loy + (float)(y + 1) * ey)));
+      const float sz = fmaxf(0.0f, fmaxf((loz + (float)z * ez) - pi.z, pi.z - (loz + (float)(z + 1) * ez)));
+      const float my = fmaxf(sy - 1.0e-3f, 0.0f), mz = fmaxf(sz - 1.0e-3f, 0.0f);
+      const float d2 = my * my + mz * mz;
+      if (d2 > r2max) continue;
+      const float xr = sqrtf(r2max - d2) + 1.0e-3f;
+      const int x0 = max((int)((pi.x - xr - lox) * ivx), 0);
+      const int x1 = min((int)((pi.x + xr - lox) * ivx), dims[0] - 1);
+      if (x0 > x1) continue;
+      const int rowc = y * dims[0] + z * dims[0] * dims[1];
+      const int b = start[rowc + x0], e = start[rowc + x1 + 1];
+      for (int base = b; base < e; base += 32) {
+        const int k = base + lane;
+        if (k >= e) continue;
+        const int j = A.cell_atoms[ab + k];
+        if (j == a) continue;
+        const float4 pj = A.pos[j];
+        if (r2_nofma(pj.x - pi.x, pj.y - pi.y, pj.z - pi.z) > r2max) continue;
+        const int d = j - a;
+        bool keep = true;
+        if (d >= -32 && d < 32) {
+          if ((mask >> (d + 32)) & 1ull) keep = false;
+        } else {
+          for (int q = 0; q < far.y; ++q) {
+            const int ent = A.far_list[far.x + q];
+            if ((ent & 0x3fffffff) == j) {
+              keep = false;
+              break;
+            }
+          }
+        }
+        if (keep) ok &= tile_insert(sh, (j - ab) >> 2, 1u << (i + 8 * ((j - ab) & 3)));
+      }
+    }
+  }
+  return __all_sync(0xffffffffu, ok);
+}
 
 // Test one candidate against every atom of the group and append the kept ones
 // to the atoms' rows (ballot compaction keeps candidate order).
@@ -653,6 +786,38 @@ __device__ __forceinline__ void group_test(const Arena& A, const GroupShared& sh
   }
 }
 
+// Tile form of group_test: the candidate's pair bits with every atom of the
+// group (same r^2 and exclusion tests) go into the group's tile table.
+__device__ __forceinline__ bool group_test_tiles(const Arena& A, GroupShared& sh, const float4 (&P)[8], int n_act,
+                                                 int a0, int ab, bool valid, int j, float4 pj, float r2max) {
+  unsigned m8 = 0u;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    if (i >= n_act) break;
+    const int ai = a0 + i;
+    bool keep = valid && j != ai;
+    if (keep) keep = !(r2_nofma(pj.x - P[i].x, pj.y - P[i].y, pj.z - P[i].z) > r2max);
+    if (keep) {
+      const int d = j - ai;
+      if (d >= -32 && d < 32) {
+        if ((sh.mask[i] >> (d + 32)) & 1ull) keep = false;
+      } else {
+        const int2 far = sh.far[i];
+        for (int q = 0; q < far.y; ++q) {
+          if ((A.far_list[far.x + q] & 0x3fffffff) == j) {
+            keep = false;
+            break;
+          }
+        }
+      }
+    }
+    if (keep) m8 |= 1u << i;
+  }
+  bool ok = true;
+  if (m8) ok = tile_insert(sh, (j - ab) >> 2, m8 << (8 * ((j - ab) & 3)));
+  return ok;
+}
+
 // Complete-mode rows of one 8-atom group, built together: the warp lists the
 // cell-row runs of the union of the group's stencils (the rows and x-runs
 // within r_list of the group's bounding box), packs their candidates into
@@ -672,6 +837,9 @@ __device__ __forceinline__ void build_group(const Arena& A, int64_t g, int exclu
   const int dims[3] = {Sp->g_dims[0], Sp->g_dims[1], Sp->g_dims[2]};
   const float r2max = Sp->rlist2;
   const int* start = A.cell_start + Sp->cell_begin;
+  // production FP32 lists are cluster-pair tiles (exclusions include the
+  // exception pairs, as in the production rows)
+  const bool tiles = exclude_exc && uses_tiles(A, *Sp);
   float4 P[8];
 #pragma unroll
   for (int i = 0; i < 8; ++i) P[i] = A.pos[a0 + min(i, n_act - 1)];
@@ -679,6 +847,14 @@ __device__ __forceinline__ void build_group(const Arena& A, int64_t g, int exclu
     sh.mask[lane] = exclude_exc ? A.mask_all[a0 + lane] : A.mask_ref[a0 + lane];
     sh.far[lane] = A.far[a0 + lane];
   }
+  if (tiles) {
+    for (int k = lane; k < kTileHash; k += 32) {
+      sh.tkey[k] = 0;
+      sh.tmask[k] = 0u;
+    }
+    if (lane == 0) sh.tcount = 0;
+  }
+  __syncwarp();
   float bl[3] = {P[0].x, P[0].y, P[0].z}, bh[3] = {P[0].x, P[0].y, P[0].z};
 #pragma unroll
   for (int i = 1; i < 8; ++i) {
@@ -698,7 +874,19 @@ __device__ __forceinline__ void build_group(const Arena& A, int64_t g, int exclu
   const int ny = y1 - y0 + 1;
   const int n_rows = (z1 - z0 + 1) * ny;
   if (n_rows > kMaxRuns) {
-    // a group that spans two distant chains: build its rows atom by atom
+    // a group that spans two distant chains: build its list atom by atom
+    if (tiles) {
+      bool ok = true;
+      for (int i = 0; i < n_act; ++i) ok &= tile_atom(A, Sp, sh, a0 + i, i, lane);
+      const int nt = ok ? tile_flush(A, sh, g, ab, lane) : -1;
+      if (nt < 0) {
+        if (lane == 0) atomicOr(&Sp->status, kStNbrOverflow);
+        return;
+      }
+      if (lane < n_act) A.xref[a0 + lane] = P[lane];
+      __syncwarp();
+      return;
+    }
     for (int i = 0; i < n_act; ++i) {
       int count = -1;
       build_row(A, a0 + i, exclude_exc, lane, &count);
@@ -757,15 +945,29 @@ __device__ __forceinline__ void build_group(const Arena& A, int64_t g, int exclu
   int j = c < total ? A.cell_atoms[ab + locate(c)] : -1;
   int j1 = c + 32 < total ? A.cell_atoms[ab + locate(c + 32)] : -1;
   float4 pj = j >= 0 ? A.pos[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+  bool tok = true;
   for (int c0 = 0; c0 < total; c0 += 32) {
     const bool valid = c < total;
     const float4 p1 = j1 >= 0 ? A.pos[j1] : make_float4(0.f, 0.f, 0.f, 0.f);
     const int j2 = c + 64 < total ? A.cell_atoms[ab + locate(c + 64)] : -1;
-    group_test(A, sh, P, n_act, a0, (int)g, valid, j, pj, r2max, exclude_exc, lt, cnt, ovf);
+    if (tiles)
+      tok &= group_test_tiles(A, sh, P, n_act, a0, ab, valid, j, pj, r2max);
+    else
+      group_test(A, sh, P, n_act, a0, (int)g, valid, j, pj, r2max, exclude_exc, lt, cnt, ovf);
     c += 32;
     j = j1;
     pj = p1;
     j1 = j2;
+  }
+  if (tiles) {
+    const int nt = __all_sync(0xffffffffu, tok) ? tile_flush(A, sh, g, ab, lane) : -1;
+    if (nt < 0) {
+      if (lane == 0) atomicOr(&Sp->status, kStNbrOverflow);
+      return;
+    }
+    if (lane < n_act) A.xref[a0 + lane] = P[lane];
+    __syncwarp();
+    return;
   }
   if (ovf) {
     if (lane == 0) atomicOr(&Sp->status, kStNbrOverflow);
@@ -785,7 +987,8 @@ __device__ __forceinline__ void build_group(const Arena& A, int64_t g, int exclu
 // queue.  Complete lists are built a group at a time; REF27 lists (parity
 // only) atom by atom with the reference's own 27-cell stencil.
 __global__ void __launch_bounds__(kNbrThreads, 3) k_nbr_build(Arena A, int64_t n_span, int exclude_exc) {
-  __shared__ GroupShared sh[kNbrThreads / 32];
+  extern __shared__ __align__(16) unsigned char nbr_smem[];
+  GroupShared* sh = reinterpret_cast<GroupShared*>(nbr_smem);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t gw = (int64_t)blockIdx.x * (kNbrThreads / 32) + warp;
   const int64_t n_warps = (int64_t)gridDim.x * (kNbrThreads / 32);
@@ -959,18 +1162,20 @@ void launch_control_cells(const Arena& A, int n_sys, int mode, int nbr_override,
 void launch_nbr_build(const Arena& A, int64_t n_atoms_span, int exclude_exceptions, cudaStream_t st,
                       bool persistent) {
   if (n_atoms_span <= 0) return;
+  const size_t smem = sizeof(GroupShared) * (kNbrThreads / 32);
   static int resident = 0;  // CTAs that fit on the GPU at once
   if (!resident) {
     int dev = 0, n_sm = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_nbr_build, kNbrThreads, 0);
+    cudaFuncSetAttribute(k_nbr_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_nbr_build, kNbrThreads, smem);
     resident = std::max(1, n_sm) * std::max(1, per_sm);
   }
   const int64_t groups = (n_atoms_span + 7) / 8;
   const int64_t per_group = (groups + kNbrThreads / 32 - 1) / (kNbrThreads / 32);
   const int grid = (int)(persistent ? std::min<int64_t>(groups, resident) : std::min<int64_t>(per_group, 1 << 30));
-  k_nbr_build<<<grid, kNbrThreads, 0, st>>>(A, n_atoms_span, exclude_exceptions);
+  k_nbr_build<<<grid, kNbrThreads, smem, st>>>(A, n_atoms_span, exclude_exceptions);
 }
 
 }  // namespace pq

@@ -26,6 +26,13 @@ __host__ __device__ __forceinline__ int64_t nbr_index(int64_t a, int k) {
   const int t = k >> 2;
   return (a >> 3) * (kNbrCap * 8) + (t >> 2) * 128 + ((((int)(a & 7) << 2) + (k & 3)) << 2) + (t & 3);
 }
+// Cluster-pair tiles (FP32 complete-mode lists): an i-cluster is an aligned
+// group of 8 consecutive atoms, a j-cluster an aligned group of 4; one tile
+// {j-cluster, 32-bit mask} says which of the 8 x 4 pairs are in the list
+// (bit i + 8 jj for atoms 8g + i and 4jc + jj).  Tiles of an i-cluster are
+// stored in ascending j-cluster order, at most kTileCap of them.
+constexpr int kTileCap = 768;
+constexpr int kTileHash = 1024;  // per-warp build table (open addressing over j-clusters)
 constexpr int kRefCellCap = 512;  // REF27 cell capacity (MAX_ATOMS_PER_CELL)
 constexpr int kRefMaxDim = 32;    // REF27 cells per axis (MAX_CELLS_PER_DIM)
 
@@ -176,6 +183,11 @@ struct Arena {
   // lists
   int* nbr = nullptr;   // tiled rows, see nbr_index()
   int* nnbr = nullptr;  // row lengths
+  // cluster-pair tiles: pair_layout 1 selects them for FP32 complete-mode
+  // systems (0: rows for every system)
+  int pair_layout = 1;
+  int2* tiles = nullptr;  // [atom_cap / 8][kTileCap] {j-cluster, mask}
+  int* ntile = nullptr;   // [atom_cap / 8] tiles per i-cluster
   int* cell_start = nullptr;  // per system: cell_cap+1 entries
   int* cell_atoms = nullptr;  // per atom (sorted by cell)
   int* atom_cell = nullptr;
@@ -194,6 +206,11 @@ struct Arena {
   double* f64 = nullptr;     // 3 planes of atom_cap
   double2* lj64 = nullptr;   // sigma/2, sqrt(eps) in double
 };
+
+// Whether a system's list is cluster-pair tiles (else neighbour rows).
+__host__ __device__ __forceinline__ bool uses_tiles(const Arena& A, const SysDev& S) {
+  return A.pair_layout == 1 && !A.fp64 && S.nbr_mode == 0;
+}
 
 // K2 modes
 constexpr int kCtlPrime = 0;  // force a rebuild, no COM, no step increment

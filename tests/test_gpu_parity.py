@@ -316,3 +316,55 @@ def test_tiny_and_ragged_systems(gpu, orc):
         solo.close()
         assert np.array_equal(x, xs) and np.array_equal(v, vs)
     b.close()
+
+
+@pytest.mark.parametrize("layout", ["rows", "tiles"])
+def test_every_force_launch_shape_gives_the_same_bits_in_each_layout(gpu, layout):
+    """Both list layouts, compact chains: each launch shape of the force
+    kernel ends 45 steps (across list rebuilds) in the same bits."""
+    topos = [gpu.Topology.polyala_compact(1, n, seed=60 + n) for n in (9, 52, 140)]
+    lay = gpu.PAIR_ROWS if layout == "rows" else gpu.PAIR_TILES
+    states = []
+    n_shapes, v = 1, 0
+    while v < n_shapes:
+        b = gpu.Batch(max_atoms=2048, max_systems=4)
+        b.set_pair_layout(lay)
+        slots = [b.add_system(t, gpu.Params(stream=k)) for k, t in enumerate(topos)]
+        n_shapes = b.set_force_variant(v)
+        assert b.pair_layout == lay
+        b.step(45)
+        states.append([b.get_state(s) for s in slots])
+        b.close()
+        v += 1
+    for other in states[1:]:
+        for (x0, v0), (x1, v1) in zip(states[0], other):
+            assert np.array_equal(x0, x1) and np.array_equal(v0, v1)
+
+
+def test_tile_and_row_layouts_hold_the_same_pairs_and_forces(gpu, orc):
+    """The cluster-pair tiles and the per-atom rows list the same pairs; their
+    forces (FP32 partial sums grouped differently) agree with each other and
+    with the FP64 oracle within the force bar, energies within the energy
+    bar, and each layout repeats its own bits."""
+    topo = gpu.Topology.polyala_compact(1, 300, seed=17)
+    p = gpu.Params()
+    out = {}
+    for name, lay in (("rows", gpu.PAIR_ROWS), ("tiles", gpu.PAIR_TILES)):
+        eng = gpu.NhsAmberFusedEngine(topo, p)
+        eng.set_pair_layout(lay)
+        pairs = eng.build_neighbors(gpu.NLIST_COMPLETE)
+        pe, f, fx = eng.compute_forces()
+        comp = eng.energy_components()
+        _, _, fx2 = eng.compute_forces()
+        assert np.array_equal(fx, fx2)
+        out[name] = (pairs, pe, f, comp)
+        eng.close()
+    assert np.array_equal(out["rows"][0], out["tiles"][0])
+    off, lst = _oracle(orc, topo, p).ref_exclusions()
+    assert np.array_equal(out["tiles"][0], orc.pairs_brute(topo.positions, 144.0, off, lst))
+    f64, e64 = _oracle(orc, topo, p).forces_f64()
+    for name in ("rows", "tiles"):
+        _, pe, f, comp = out[name]
+        assert rel_rms(f, f64) <= FORCE_RTOL, name
+        assert abs(pe - e64.sum()) <= ENERGY_RTOL * abs(e64).sum(), name
+    assert rel_rms(out["tiles"][2], out["rows"][2]) <= 1e-6

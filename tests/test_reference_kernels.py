@@ -204,6 +204,33 @@ def test_half_kick_bit_exact_with_reference(pq, orc, ref, sysx, gamma):
     assert np.array_equal(v_ref, v_orc)
 
 
+@pytest.mark.parametrize("gamma,dt,temperature", [(1.0, 0.004, 300.0), (5.0, 0.002, 250.0), (1000.0, 0.004, 300.0)])
+def test_ou_half_step_bit_exact_with_reference(pq, orc, ref, sysx, gamma, dt, temperature):
+    """The OU half-step (langevin_thermostat as the OU phases call it) from
+    the reference's own cuRAND draws: given the normals it drew and its c1,
+    the oracle's OU update, which the production integrator reproduces bit
+    for bit with its own (Philox) normals, equals the reference's.  The
+    library's c1, exp(-γ dt/2) in binary64 rounded to float, is within one
+    float ulp of the device expf the reference evaluates."""
+    topo, x = sysx
+    v = _thermal(topo, 7)
+    v_ref, z, c1_ref = ref.ou(v, topo.masses, temperature, gamma, dt, seed=0x5052_4953_4d5f_4d42)
+    assert np.isfinite(z).all() and 0.5 < float(np.std(z)) < 1.5  # the draws are standard normals
+    o = _orc(orc, topo, gamma=gamma, dt=dt, temperature=temperature)
+    o.set_state(x, v)
+    o.ou_all(z, c1_ref)
+    _, v_orc = o.get_state()
+    o.close()
+    assert np.array_equal(v_ref, v_orc)
+    c1_lib = np.float32(orc.c1_of(gamma, dt))
+    assert abs(int(c1_lib.view(np.int32)) - int(np.float32(c1_ref).view(np.int32))) <= 1
+    # with the reference's own compiler flags (FMA contraction on) the update
+    # differs from the uncontracted one by rounding only
+    v_fma, z2, _ = ref.ou(v, topo.masses, temperature, gamma, dt, seed=0x5052_4953_4d5f_4d42, nofma=False)
+    assert np.array_equal(z, z2)
+    assert rel_rms(v_fma, v_ref) <= 1e-6
+
+
 def test_rattle_bit_exact_with_reference(pq, orc, ref, sysx):
     topo, _ = sysx
     x = topo.positions  # constrained geometry
