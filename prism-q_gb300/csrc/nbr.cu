@@ -687,7 +687,8 @@ __device__ int tile_flush(const Arena& A, GroupShared& sh, int64_t g, int ab, in
 
 // Tiles input of one atom (i of the group) from its own stencil, as
 // build_row scans it: used for a group whose union stencil is too large.
-__device__ bool tile_atom(const Arena& A, const SysDev* Sp, GroupShared& sh, int a, int i, int lane) {
+__device__ bool tile_atom(const Arena& A, const SysDev* Sp, GroupShared& sh, int a, int i, int lane,
+                          int exclude_exc) {
   const int ab = Sp->atom_begin;
   const int dims[3] = {Sp->g_dims[0], Sp->g_dims[1], Sp->g_dims[2]};
   const float r2max = Sp->rlist2;
@@ -695,7 +696,7 @@ __device__ bool tile_atom(const Arena& A, const SysDev* Sp, GroupShared& sh, int
   const float4 pi = A.pos[a];
   const int cell = A.atom_cell[a];
   const int cx = cell % dims[0], cy = (cell / dims[0]) % dims[1], cz = cell / (dims[0] * dims[1]);
-  const unsigned long long mask = A.mask_all[a];
+  const unsigned long long mask = exclude_exc ? A.mask_all[a] : A.mask_ref[a];
   const int2 far = A.far[a];
   const float lox = Sp->g_lo[0], loy = Sp->g_lo[1], loz = Sp->g_lo[2];
   const float ivx = Sp->g_inv_edge[0];
@@ -732,7 +733,7 @@ __device__ bool tile_atom(const Arena& A, const SysDev* Sp, GroupShared& sh, int
         } else {
           for (int q = 0; q < far.y; ++q) {
             const int ent = A.far_list[far.x + q];
-            if ((ent & 0x3fffffff) == j) {
+            if ((ent & 0x3fffffff) == j && (exclude_exc || !(ent & 0x40000000))) {
               keep = false;
               break;
             }
@@ -789,7 +790,8 @@ __device__ __forceinline__ void group_test(const Arena& A, const GroupShared& sh
 // Tile form of group_test: the candidate's pair bits with every atom of the
 // group (same r^2 and exclusion tests) go into the group's tile table.
 __device__ __forceinline__ bool group_test_tiles(const Arena& A, GroupShared& sh, const float4 (&P)[8], int n_act,
-                                                 int a0, int ab, bool valid, int j, float4 pj, float r2max) {
+                                                 int a0, int ab, bool valid, int j, float4 pj, float r2max,
+                                                 int exclude_exc) {
   unsigned m8 = 0u;
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
@@ -804,7 +806,8 @@ __device__ __forceinline__ bool group_test_tiles(const Arena& A, GroupShared& sh
       } else {
         const int2 far = sh.far[i];
         for (int q = 0; q < far.y; ++q) {
-          if ((A.far_list[far.x + q] & 0x3fffffff) == j) {
+          const int ent = A.far_list[far.x + q];
+          if ((ent & 0x3fffffff) == j && (exclude_exc || !(ent & 0x40000000))) {
             keep = false;
             break;
           }
@@ -837,9 +840,10 @@ __device__ __forceinline__ void build_group(const Arena& A, int64_t g, int exclu
   const int dims[3] = {Sp->g_dims[0], Sp->g_dims[1], Sp->g_dims[2]};
   const float r2max = Sp->rlist2;
   const int* start = A.cell_start + Sp->cell_begin;
-  // production FP32 lists are cluster-pair tiles (exclusions include the
-  // exception pairs, as in the production rows)
-  const bool tiles = exclude_exc && uses_tiles(A, *Sp);
+  // FP32 complete-mode lists are cluster-pair tiles (the production build
+  // excludes the exception pairs, the parity build of prismq_build_neighbors
+  // keeps them, as for rows)
+  const bool tiles = uses_tiles(A, *Sp);
   float4 P[8];
 #pragma unroll
   for (int i = 0; i < 8; ++i) P[i] = A.pos[a0 + min(i, n_act - 1)];
@@ -877,7 +881,7 @@ __device__ __forceinline__ void build_group(const Arena& A, int64_t g, int exclu
     // a group that spans two distant chains: build its list atom by atom
     if (tiles) {
       bool ok = true;
-      for (int i = 0; i < n_act; ++i) ok &= tile_atom(A, Sp, sh, a0 + i, i, lane);
+      for (int i = 0; i < n_act; ++i) ok &= tile_atom(A, Sp, sh, a0 + i, i, lane, exclude_exc);
       const int nt = ok ? tile_flush(A, sh, g, ab, lane) : -1;
       if (nt < 0) {
         if (lane == 0) atomicOr(&Sp->status, kStNbrOverflow);
@@ -951,7 +955,7 @@ __device__ __forceinline__ void build_group(const Arena& A, int64_t g, int exclu
     const float4 p1 = j1 >= 0 ? A.pos[j1] : make_float4(0.f, 0.f, 0.f, 0.f);
     const int j2 = c + 64 < total ? A.cell_atoms[ab + locate(c + 64)] : -1;
     if (tiles)
-      tok &= group_test_tiles(A, sh, P, n_act, a0, ab, valid, j, pj, r2max);
+      tok &= group_test_tiles(A, sh, P, n_act, a0, ab, valid, j, pj, r2max, exclude_exc);
     else
       group_test(A, sh, P, n_act, a0, (int)g, valid, j, pj, r2max, exclude_exc, lt, cnt, ovf);
     c += 32;
