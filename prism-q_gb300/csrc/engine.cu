@@ -1460,6 +1460,16 @@ prismq_status batch_admit(prismq_batch* B, const Lowered& L0, const prismq_param
   }
   PQ_CK(cudaMemsetAsync(A.nnbr + ab, 0, sizeof(int) * L.n, st));
   PQ_CK(cudaMemsetAsync(A.ntile + ab / 8, 0, sizeof(int) * ((L.n + 7) / 8), st));
+  {
+    // the atoms between the system's end and the next 32-atom boundary belong
+    // to no system; tiles read them as the tail of the last j-cluster (with
+    // no pair bit set), so they hold finite zeros
+    const int64_t pad = ((ab + L.n + 31) / 32) * 32 - (ab + L.n);
+    if (pad > 0) {
+      PQ_CK(cudaMemsetAsync(A.pos + ab + L.n, 0, sizeof(float4) * pad, st));
+      PQ_CK(cudaMemsetAsync(A.lj + ab + L.n, 0, sizeof(float2) * pad, st));
+    }
+  }
   PQ_CK(cudaMemsetAsync(A.f + ab, 0, sizeof(long long) * L.n, st));
   PQ_CK(cudaMemsetAsync(A.f + A.atom_cap + ab, 0, sizeof(long long) * L.n, st));
   PQ_CK(cudaMemsetAsync(A.f + 2 * A.atom_cap + ab, 0, sizeof(long long) * L.n, st));

@@ -454,23 +454,35 @@ __device__ __forceinline__ void force_tiles(const Arena& A, int64_t n_span, int 
   for (int t0 = 0; t0 < nt; t0 += 32) {
     const int2 e = t0 + lane < nt ? __ldg(tl + t0 + lane) : make_int2(0, 0);
     const int m = min(32, nt - t0);
+    // software pipeline: the next tile's j atom is loaded while this one is
+    // evaluated
+    unsigned bits_n = (unsigned)__shfl_sync(0xffffffffu, e.y, 0);
+    int j_n = (__shfl_sync(0xffffffffu, e.x, 0) << 2) + q;
+    float4 pj_n = __ldg(A.pos + j_n);
+    float2 lj_n = __ldg(A.lj + j_n);
     for (int u = 0; u < m; ++u) {
-      const int jc = __shfl_sync(0xffffffffu, e.x, u);
-      const unsigned bits = (unsigned)__shfl_sync(0xffffffffu, e.y, u);
-      const int j = (jc << 2) + q;
-      const float4 pj = __ldg(A.pos + j);
+      const unsigned bits = bits_n;
+      const float4 pj = pj_n;
+      const float2 lj = lj_n;
+      if (u + 1 < m) {
+        bits_n = (unsigned)__shfl_sync(0xffffffffu, e.y, u + 1);
+        j_n = (__shfl_sync(0xffffffffu, e.x, u + 1) << 2) + q;
+        pj_n = __ldg(A.pos + j_n);
+        lj_n = __ldg(A.lj + j_n);
+      }
       const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
       const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
       const bool in = (bits & lanebit) != 0u && r2 < cut2 && r2 >= kMinPairR2;
       if (__any_sync(0xffffffffu, in)) {
-        const float2 lj = __ldg(A.lj + j);
+        // lanes outside the list or the cutoff add an exact zero (the j atoms
+        // past a system's end hold finite positions: admission zeroes them)
         const float sig = li.x + lj.x, eps = li.y * lj.y, qq = qi * pj.w;
         float inv_r, s6;
         float fs = pair_scalar<float>(fmaxf(r2, kMinPairR2), sig, eps, qq, inv_r, s6);
         fs = in ? fs : 0.0f;
-        f.x -= fs * (in ? dx : 0.0f);
-        f.y -= fs * (in ? dy : 0.0f);
-        f.z -= fs * (in ? dz : 0.0f);
+        f.x -= fs * dx;
+        f.y -= fs * dy;
+        f.z -= fs * dz;
         if (kEnergy && in) {
           const float sc2 = sig * sig * inv_rc * inv_rc;
           const float sc6 = sc2 * sc2 * sc2;
@@ -768,7 +780,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_force(Arena A, int64_t n_sp
 struct ForceShape {
   int block, min_blocks;
 };
-static const ForceShape kForceShapes[] = {{128, 1}, {128, 8}, {128, 12}};
+static const ForceShape kForceShapes[] = {{128, 1}, {128, 8}, {128, 10}, {128, 12}};
 
 int force_variant_count() { return (int)(sizeof(kForceShapes) / sizeof(kForceShapes[0])); }
 
@@ -808,7 +820,8 @@ void launch_force(const Arena& A, int64_t n_atoms_span, bool energy, cudaStream_
   }
   switch (variant) {
     case 1: force_launch<float, false, 8>(A, n_atoms_span, ob, cap, st); break;
-    case 2: force_launch<float, false, 12>(A, n_atoms_span, ob, cap, st); break;
+    case 2: force_launch<float, false, 10>(A, n_atoms_span, ob, cap, st); break;
+    case 3: force_launch<float, false, 12>(A, n_atoms_span, ob, cap, st); break;
     default: force_launch<float, false, 1>(A, n_atoms_span, ob, cap, st); break;
   }
 }
