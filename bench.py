@@ -68,8 +68,8 @@ def args_parse():
     ap.add_argument("--cpu-systems", type=int, default=16,
                     help="stratified systems of the workload that the CPU legs time")
     ap.add_argument("--cpu-steps", type=int, default=20, help="steps the device arm's CPU-baseline leg times")
-    ap.add_argument("--pair-layout", default="tiles", choices=["tiles", "rows"],
-                    help="production neighbour-list layout: cluster-pair tiles (default) or per-atom rows")
+    ap.add_argument("--pair-layout", default="rows", choices=["rows", "tiles"],
+                    help="production neighbour-list layout: per-atom rows (default) or cluster-pair tiles")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving leg of the default run")
     ap.add_argument("--serve-jobs", type=int, default=200)
     ap.add_argument("--serve-rate", type=float, default=50.0, help="Poisson arrival rate, jobs/s")
@@ -618,8 +618,10 @@ def run_ours(args, pq, rank, world):
     clocks.start()
     total_ms = ctypes.c_float()
     phase_ms = (ctypes.c_float * (5 * args.steps))()
+    torch.cuda.nvtx.range_push("timed")  # the launches a profiler of the timed region selects
     rc = pq.load().prismq_batch_run_timed(batch.h, args.steps, ctypes.addressof(total_ms),
                                           ctypes.addressof(phase_ms))
+    torch.cuda.nvtx.range_pop()
     if rc:
         raise pq.PrismQError(rc, pq.load().prismq_last_error().decode())
     clk = clocks.stop()

@@ -416,11 +416,11 @@ prismq_status prismq_batch_frames_configure(prismq_batch* b, int32_t slot, int32
 prismq_status prismq_batch_frames_read(prismq_batch* b, int32_t slot, float* xyz, float* vxyz, int64_t* steps,
                                        int32_t max_frames, int32_t* n_out, int64_t* dropped);
 /* Layout of the production neighbour list (FP32 systems in complete mode):
- *   1 (default) cluster-pair tiles: i-clusters of 8 consecutive atoms against
+ *   0 (default) one row of partner indices per atom (at most 1024), the
+ *     layout REF27 and FP64 runs always use;
+ *   1 cluster-pair tiles: i-clusters of 8 consecutive atoms against
  *     j-clusters of 4, one {j-cluster, 32-bit pair mask} per tile, the tiles
- *     of an i-cluster in ascending j-cluster order (at most 768);
- *   0 one row of partner indices per atom (at most 1024), the layout REF27
- *     and FP64 runs always use.
+ *     of an i-cluster in ascending j-cluster order (at most 768).
  * The pair set is the same; the forces differ only in the grouping of their
  * FP32 partial sums, and each layout is bit-reproducible on its own.  Setting
  * it rebuilds every resident system's list before the next step, so set it

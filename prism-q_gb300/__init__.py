@@ -688,7 +688,7 @@ class NhsAmberFusedEngine:
         return self.build_neighbors(NLIST_REF27)
 
     def set_pair_layout(self, layout: int) -> None:
-        """PAIR_TILES (default) or PAIR_ROWS for the production list; set before stepping."""
+        """PAIR_ROWS (default) or PAIR_TILES for the production list; set before stepping."""
         _check(load().prismq_set_pair_layout(self.h, int(layout)))
 
     def debug_phases(self, which: int, step: int) -> None:
@@ -824,7 +824,7 @@ class Batch:
                                              _ptr(vxyz_out)))
 
     def set_pair_layout(self, layout: int) -> None:
-        """PAIR_TILES (default) or PAIR_ROWS for the production list; set before stepping."""
+        """PAIR_ROWS (default) or PAIR_TILES for the production list; set before stepping."""
         _check(load().prismq_batch_set_pair_layout(self.h, int(layout)))
 
     @property

@@ -2,7 +2,9 @@
 
 Each translation unit is compiled in parallel with nvcc; the integrator and
 the neighbour/control kernels are compiled with --fmad=false so that their
-floating-point results match the CPU oracle bit for bit, and host code is
+floating-point results match the CPU oracle bit for bit, the force kernels
+with --fmad=false and explicit FMAs so that no launch shape can fuse them
+differently, and host code is
 compiled with -ffp-contract=off for the same reason (gcc contracts a*b+c into
 FMA by default on aarch64).
 """
@@ -27,7 +29,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-DNDEBUG", f"-I{INCLUDE}", f"-I{CSR
 
 UNITS = {
     "engine.cu": [],
-    "force.cu": [],
+    "force.cu": ["--fmad=false"],
     "integrate.cu": ["--fmad=false"],
     "nbr.cu": ["--fmad=false"],
     "noalloc.cu": ["--fmad=false"],

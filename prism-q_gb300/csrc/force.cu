@@ -207,15 +207,26 @@ __device__ __forceinline__ void dihedral_term(const R4<R>* pos, const DihT d, in
 }
 
 // ---- pair law: force on i from j (d = xj - xi), LJ + Coulomb ----
+// The file is compiled without FMA contraction, so every fused multiply-add
+// is written out: the compiler cannot fuse differently in different launch
+// shapes (register budgets), and every shape gives the same bits.
 template <class R>
 __device__ __forceinline__ R pair_scalar(R r2, R sig, R eps, R qq, R& inv_r, R& s6) {
   inv_r = inv_sqrt_r(r2);
   const R inv_r2 = inv_r * inv_r;
   const R s2 = sig * sig * inv_r2;
   s6 = s2 * s2 * s2;
-  const R flj = R(24.0f) * eps * inv_r2 * (R(2.0f) * s6 * s6 - s6);
+  const R u = fma_r(R(2.0f) * s6, s6, -s6);            // 2 s6^2 - s6
   const R fc = R(kCoulomb) * qq * inv_r2 * inv_r;
-  return flj + fc;
+  return fma_r(R(24.0f) * eps * inv_r2, u, fc);        // 24 eps/r^2 (2 s6^2 - s6) + qq k/r^3
+}
+
+// f -= fs * d, one rounding per component.
+template <class R>
+__device__ __forceinline__ void acc_pair(Acc<R>& f, R fs, R dx, R dy, R dz) {
+  f.x = fma_r(-fs, dx, f.x);
+  f.y = fma_r(-fs, dy, f.y);
+  f.z = fma_r(-fs, dz, f.z);
 }
 
 // Sum over the 4 lanes of one atom (fixed butterfly: exact for int64,
@@ -243,9 +254,7 @@ __device__ __forceinline__ void pair_accumulate(const R4<R> pi, R qi, R2<R> li, 
   R inv_r, s6;
   R fs = pair_scalar<R>(max_r(r2, R(kMinPairR2)), sig, eps, qq, inv_r, s6);
   fs = in ? fs : R(0.0f);
-  f.x -= fs * dx;
-  f.y -= fs * dy;
-  f.z -= fs * dz;
+  acc_pair<R>(f, fs, dx, dy, dz);
 }
 
 __device__ __forceinline__ void store_force(const Arena& A, int a, const Acc<float>& f) {
@@ -454,35 +463,23 @@ __device__ __forceinline__ void force_tiles(const Arena& A, int64_t n_span, int 
   for (int t0 = 0; t0 < nt; t0 += 32) {
     const int2 e = t0 + lane < nt ? __ldg(tl + t0 + lane) : make_int2(0, 0);
     const int m = min(32, nt - t0);
-    // software pipeline: the next tile's j atom is loaded while this one is
-    // evaluated
-    unsigned bits_n = (unsigned)__shfl_sync(0xffffffffu, e.y, 0);
-    int j_n = (__shfl_sync(0xffffffffu, e.x, 0) << 2) + q;
-    float4 pj_n = __ldg(A.pos + j_n);
-    float2 lj_n = __ldg(A.lj + j_n);
     for (int u = 0; u < m; ++u) {
-      const unsigned bits = bits_n;
-      const float4 pj = pj_n;
-      const float2 lj = lj_n;
-      if (u + 1 < m) {
-        bits_n = (unsigned)__shfl_sync(0xffffffffu, e.y, u + 1);
-        j_n = (__shfl_sync(0xffffffffu, e.x, u + 1) << 2) + q;
-        pj_n = __ldg(A.pos + j_n);
-        lj_n = __ldg(A.lj + j_n);
-      }
+      const int jc = __shfl_sync(0xffffffffu, e.x, u);
+      const unsigned bits = (unsigned)__shfl_sync(0xffffffffu, e.y, u);
+      const int j = (jc << 2) + q;
+      const float4 pj = __ldg(A.pos + j);
       const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
       const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
       const bool in = (bits & lanebit) != 0u && r2 < cut2 && r2 >= kMinPairR2;
       if (__any_sync(0xffffffffu, in)) {
         // lanes outside the list or the cutoff add an exact zero (the j atoms
         // past a system's end hold finite positions: admission zeroes them)
+        const float2 lj = __ldg(A.lj + j);
         const float sig = li.x + lj.x, eps = li.y * lj.y, qq = qi * pj.w;
         float inv_r, s6;
         float fs = pair_scalar<float>(fmaxf(r2, kMinPairR2), sig, eps, qq, inv_r, s6);
         fs = in ? fs : 0.0f;
-        f.x -= fs * dx;
-        f.y -= fs * dy;
-        f.z -= fs * dz;
+        acc_pair<float>(f, fs, dx, dy, dz);
         if (kEnergy && in) {
           const float sc2 = sig * sig * inv_rc * inv_rc;
           const float sc6 = sc2 * sc2 * sc2;
@@ -741,9 +738,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_force(Arena A, int64_t n_sp
           const R sig = li.x + lj.x, eps = li.y * lj.y, qq = qi * pj.w;
           R inv_r, s6;
           const R fs = pair_scalar<R>(r2, sig, eps, qq, inv_r, s6);
-          f.x -= fs * dx;
-          f.y -= fs * dy;
-          f.z -= fs * dz;
+          acc_pair<R>(f, fs, dx, dy, dz);
           if (kEnergy) {
             const R sc2 = sig * sig * inv_rc * inv_rc;
             const R sc6 = sc2 * sc2 * sc2;

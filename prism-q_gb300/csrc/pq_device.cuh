@@ -184,8 +184,8 @@ struct Arena {
   int* nbr = nullptr;   // tiled rows, see nbr_index()
   int* nnbr = nullptr;  // row lengths
   // cluster-pair tiles: pair_layout 1 selects them for FP32 complete-mode
-  // systems (0: rows for every system)
-  int pair_layout = 1;
+  // systems (0, the default: rows for every system)
+  int pair_layout = 0;
   int2* tiles = nullptr;  // [atom_cap / 8][kTileCap] {j-cluster, mask}
   int* ntile = nullptr;   // [atom_cap / 8] tiles per i-cluster
   int* cell_start = nullptr;  // per system: cell_cap+1 entries
