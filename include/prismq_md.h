@@ -430,9 +430,9 @@ prismq_status prismq_batch_set_pair_layout(prismq_batch* b, int32_t layout);
 int32_t prismq_batch_pair_layout(const prismq_batch* b);
 prismq_status prismq_set_pair_layout(prismq_system* sys, int32_t layout);
 /* The autotuner's choice for the batch's force kernel: out[0] = variant
- * (-1 before the first step), out[1] = threads per block, out[2] = minimum
- * resident blocks per SM given to the register allocator.  The launch shape
- * does not change results. */
+ * (-1 before the first step), out[1] = threads per block (four per atom: 128
+ * for 32 atoms, 256 for 64), out[2] = minimum resident blocks per SM given to
+ * the register allocator.  The launch shape does not change results. */
 prismq_status prismq_batch_tuning(prismq_batch* b, int32_t out[3]);
 /* Pin the force kernel's launch shape to `variant` (0 .. n-1; *n_variants
  * receives n, may be NULL), or hand the choice back to the autotuner with

@@ -537,8 +537,12 @@ __device__ __forceinline__ void force_tiles(const Arena& A, int64_t n_span, int 
 // is identical whatever batch it is computed in.  The reference recomputes
 // each term for every member atom (nhs_amber_fused.cu:3002-3090); evaluating
 // it once per group gives each member the same contribution.
-template <class R, bool kEnergy, int kMinBlocks>
-__global__ void __launch_bounds__(128, kMinBlocks) k_force(Arena A, int64_t n_span, int sel, int cap) {
+//
+// A block holds kG such groups (128 threads each, consecutive groups); the
+// groups share nothing but the block's barriers, so kG changes the launch
+// shape, never the results.
+template <class R, bool kEnergy, int kMinBlocks, int kG>
+__global__ void __launch_bounds__(128 * kG, kMinBlocks) k_force(Arena A, int64_t n_span, int sel, int cap) {
   // the row builder that ran before this launch consumed the rebuild queue
   // (the branch-B launch of an overlapped step may run beside that builder)
   if (sel != kSelBranchB && blockIdx.x == 0 && threadIdx.x == 0) {
@@ -546,23 +550,32 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_force(Arena A, int64_t n_sp
     A.work_ctl[1] = 0;
   }
   extern __shared__ __align__(16) unsigned char force_smem[];
-  __shared__ int s_base[kForceGroup], s_nb[kForceGroup], s_na[kForceGroup], s_nd[kForceGroup];
-  const int tid = threadIdx.x, q = tid & 3;
-  const int64_t a0 = (int64_t)blockIdx.x * kForceGroup;
-  if (a0 >= n_span) return;
-  const int s0 = A.atom_sys[a0];
-  if (s0 < 0) return;
-  const SysDev* Sp = &A.sys[s0];
-  if (!Sp->active) return;  // whole block leaves together
-  if (sel == kSelRebuilding && !Sp->rebuilding) return;
-  if (sel == kSelBranchA && !Sp->branch_a) return;
-  if (sel == kSelBranchB && Sp->branch_a) return;
-  R* slot_x = reinterpret_cast<R*>(force_smem);
+  __shared__ int s_base_g[kG][kForceGroup], s_nb_g[kG][kForceGroup], s_na_g[kG][kForceGroup],
+      s_nd_g[kG][kForceGroup];
+  const int sub = threadIdx.x >> 7;  // the block's group this thread works on
+  const int tid = threadIdx.x & 127, q = tid & 3;
+  int* s_base = s_base_g[sub];
+  int* s_nb = s_nb_g[sub];
+  int* s_na = s_na_g[sub];
+  int* s_nd = s_nd_g[sub];
+  const int64_t gi = (int64_t)blockIdx.x * kG + sub;
+  const int64_t a0 = gi * kForceGroup;
+  // a group with nothing to do skips its work but still meets the barriers
+  bool skip = a0 >= n_span;
+  const int s0 = skip ? -1 : A.atom_sys[a0];
+  skip = skip || s0 < 0;
+  const SysDev* Sp = skip ? nullptr : &A.sys[s0];
+  if (!skip) {
+    skip = !Sp->active || (sel == kSelRebuilding && !Sp->rebuilding) || (sel == kSelBranchA && !Sp->branch_a) ||
+           (sel == kSelBranchB && Sp->branch_a);
+  }
+  const size_t slot_bytes = (size_t)cap * (3 * sizeof(R) + (kEnergy ? sizeof(double) : 0));
+  R* slot_x = reinterpret_cast<R*>(force_smem + sub * slot_bytes);
   R* slot_y = slot_x + cap;
   R* slot_z = slot_y + cap;
   double* slot_e = reinterpret_cast<double*>(slot_z + cap);
   // ---- slot layout of the group's atoms ----
-  if (tid < kForceGroup) {
+  if (!skip && tid < kForceGroup) {
     const int64_t b = a0 + tid;
     int nb = 0, na = 0, nd = 0, ne = 0;
     if (b < n_span && A.atom_sys[b] == s0) {
@@ -586,7 +599,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_force(Arena A, int64_t n_sp
   __syncthreads();
   const R4<R>* pos = positions(A, R(0));
   // ---- every term with a member in the group, once ----
-  const int2 gr = A.grp[blockIdx.x];
+  const int2 gr = skip ? make_int2(0, 0) : A.grp[gi];
   bool bad = false;
   for (int r = tid; r < gr.y; r += 128) {
     const int ref = A.grp_refs[gr.x + r];
@@ -634,6 +647,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_force(Arena A, int64_t n_sp
   }
   if (bad) atomicOr(&A.sys[s0].status, kStNonfinite);
   __syncthreads();
+  if (skip) return;
   if constexpr (sizeof(R) == 4) {
     if (uses_tiles(A, *Sp)) {
       force_tiles<kEnergy>(A, n_span, s0, Sp, a0, tid, reinterpret_cast<const float*>(slot_x),
@@ -769,13 +783,15 @@ __global__ void __launch_bounds__(128, kMinBlocks) k_force(Arena A, int64_t n_sp
   }
 }
 
-// Launch shapes of the force-only kernel the autotuner chooses from: the
-// minimum resident 128-thread blocks per SM handed to the register allocator.
-// The shape changes neither the per-atom decomposition nor the results.
+// Launch shapes of the force-only kernel the autotuner chooses from: atoms
+// per block (32 or 64: one or two force groups) and the minimum resident
+// blocks per SM handed to the register allocator.  The shape changes neither
+// the per-atom decomposition nor the results.
 struct ForceShape {
   int block, min_blocks;
 };
-static const ForceShape kForceShapes[] = {{128, 1}, {128, 8}, {128, 10}, {128, 12}};
+static const ForceShape kForceShapes[] = {{128, 1}, {128, 8}, {128, 10}, {128, 12},
+                                          {256, 4}, {256, 5}, {256, 6}};
 
 int force_variant_count() { return (int)(sizeof(kForceShapes) / sizeof(kForceShapes[0])); }
 
@@ -784,17 +800,18 @@ void force_variant_shape(int v, int* block, int* min_blocks) {
   *min_blocks = kForceShapes[v].min_blocks;
 }
 
-template <class R, bool kEnergy, int kMinBlocks>
+template <class R, bool kEnergy, int kMinBlocks, int kG = 1>
 static void force_launch(const Arena& A, int64_t n, int ob, int cap, cudaStream_t st) {
-  const size_t smem = (size_t)cap * (3 * sizeof(R) + (kEnergy ? sizeof(double) : 0));
+  const size_t smem = (size_t)kG * cap * (3 * sizeof(R) + (kEnergy ? sizeof(double) : 0));
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_force<R, kEnergy, kMinBlocks>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)((size_t)kMaxGroupSlots * (3 * sizeof(R) + sizeof(double))));
+    cudaFuncSetAttribute(k_force<R, kEnergy, kMinBlocks, kG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)((size_t)kG * kMaxGroupSlots * (3 * sizeof(R) + sizeof(double))));
     attr = true;
   }
-  const unsigned blocks = (unsigned)((n + kForceGroup - 1) / kForceGroup);
-  k_force<R, kEnergy, kMinBlocks><<<blocks, 128, smem, st>>>(A, n, ob, cap);
+  const int64_t groups = (n + kForceGroup - 1) / kForceGroup;
+  const unsigned blocks = (unsigned)((groups + kG - 1) / kG);
+  k_force<R, kEnergy, kMinBlocks, kG><<<blocks, 128 * kG, smem, st>>>(A, n, ob, cap);
 }
 
 void launch_force(const Arena& A, int64_t n_atoms_span, bool energy, cudaStream_t st, int sel, int variant,
@@ -817,6 +834,9 @@ void launch_force(const Arena& A, int64_t n_atoms_span, bool energy, cudaStream_
     case 1: force_launch<float, false, 8>(A, n_atoms_span, ob, cap, st); break;
     case 2: force_launch<float, false, 10>(A, n_atoms_span, ob, cap, st); break;
     case 3: force_launch<float, false, 12>(A, n_atoms_span, ob, cap, st); break;
+    case 4: force_launch<float, false, 4, 2>(A, n_atoms_span, ob, cap, st); break;
+    case 5: force_launch<float, false, 5, 2>(A, n_atoms_span, ob, cap, st); break;
+    case 6: force_launch<float, false, 6, 2>(A, n_atoms_span, ob, cap, st); break;
     default: force_launch<float, false, 1>(A, n_atoms_span, ob, cap, st); break;
   }
 }
