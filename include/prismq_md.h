@@ -434,6 +434,11 @@ prismq_status prismq_set_pair_layout(prismq_system* sys, int32_t layout);
  * for 32 atoms, 256 for 64), out[2] = minimum resident blocks per SM given to
  * the register allocator.  The launch shape does not change results. */
 prismq_status prismq_batch_tuning(prismq_batch* b, int32_t out[3]);
+/* The same with out[3] = atoms per block and out[4] = how many row-index
+ * iterations ahead the kernel asks L2 for the atom's row (0: no prefetch).
+ * No counterpart in the reference (its launch shape is fixed, one thread per
+ * atom, fused_engine.rs:19268-19350). */
+prismq_status prismq_batch_tuning_ex(prismq_batch* b, int32_t out[5]);
 /* Pin the force kernel's launch shape to `variant` (0 .. n-1; *n_variants
  * receives n, may be NULL), or hand the choice back to the autotuner with
  * variant -1.  Every shape gives the same bits. */

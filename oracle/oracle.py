@@ -10,6 +10,7 @@ import ctypes
 import os
 import pathlib
 import subprocess
+import threading
 
 import numpy as np
 
@@ -35,7 +36,7 @@ def build(force: bool = False) -> pathlib.Path:
     if not force and LIB.exists() and all(LIB.stat().st_mtime >= d.stat().st_mtime for d in deps):
         return LIB
     BUILD.mkdir(exist_ok=True)
-    tmp = LIB.with_suffix(".so.tmp")
+    tmp = LIB.with_suffix(f".so.{os.getpid()}.{threading.get_ident()}.tmp")
     cmd = ["gcc", *FLAGS, "-o", str(tmp), str(SRC), "-lm"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
@@ -52,7 +53,7 @@ def build_gen(force: bool = False) -> pathlib.Path:
     if not force and GEN_LIB.exists() and all(GEN_LIB.stat().st_mtime >= d.stat().st_mtime for d in deps):
         return GEN_LIB
     BUILD.mkdir(exist_ok=True)
-    tmp = GEN_LIB.with_suffix(".so.tmp")
+    tmp = GEN_LIB.with_suffix(f".so.{os.getpid()}.{threading.get_ident()}.tmp")
     cmd = ["g++", *GEN_FLAGS, "-o", str(tmp), *map(str, GEN_SRC)]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
@@ -62,6 +63,17 @@ def build_gen(force: bool = False) -> pathlib.Path:
 
 
 _gen = None
+_gen_lock = threading.Lock()
+
+
+def _load_gen() -> ctypes.CDLL:
+    G = ctypes.CDLL(str(build_gen()))
+    G.orcgen_polyala.restype = ctypes.c_void_p
+    G.orcgen_polyala.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong, ctypes.c_double,
+                                 ctypes.c_double, ctypes.c_int, ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int]
+    G.orcgen_view.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    G.orcgen_free.argtypes = [ctypes.c_void_p]
+    return G
 
 
 def polyala(n_chains: int, n_residues: int, seed: int, density: float = 0.0, box_edge: float = 0.0,
@@ -72,29 +84,25 @@ def polyala(n_chains: int, n_residues: int, seed: int, density: float = 0.0, box
     global _gen
     import importlib
 
-    if _gen is None:
-        G = ctypes.CDLL(str(build_gen()))
-        G.orcgen_polyala.restype = ctypes.c_void_p
-        G.orcgen_polyala.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong, ctypes.c_double,
-                                     ctypes.c_double, ctypes.c_int, ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int]
-        G.orcgen_view.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
-        G.orcgen_free.argtypes = [ctypes.c_void_p]
-        _gen = G
+    with _gen_lock:  # the first callers may come from several threads at once
+        if _gen is None:
+            _gen = _load_gen()
+    G = _gen
     pkg = importlib.import_module("prism-q_gb300")
     st = (ctypes.c_double * 4)()
     err = ctypes.create_string_buffer(256)
     if not compact and not (density > 0.0):
         density = 0.03
-    h = _gen.orcgen_polyala(n_chains, n_residues, seed, float(np.float32(density)), float(np.float32(box_edge)),
+    h = G.orcgen_polyala(n_chains, n_residues, seed, float(np.float32(density)), float(np.float32(box_edge)),
                             1 if compact else 0, st, err, 256)
     if not h:
         raise RuntimeError(err.value.decode())
     try:
         t = pkg.TopologyStruct()
-        _gen.orcgen_view(h, ctypes.byref(t))
+        G.orcgen_view(h, ctypes.byref(t))
         topo = pkg.Topology.from_struct(t)
     finally:
-        _gen.orcgen_free(h)
+        G.orcgen_free(h)
     if stats is not None:
         stats.update(iterations=int(st[0]), max_overlap=st[1], max_outside=st[2], min_nonbonded=st[3])
     return topo

@@ -781,10 +781,10 @@ class Batch:
 
     def tuning(self) -> dict:
         """The autotuner's force-kernel launch shape for this batch."""
-        out = np.zeros(3, np.int32)
-        _check(load().prismq_batch_tuning(self.h, _ptr(out)))
-        return {"variant": int(out[0]), "block": int(out[1]), "atoms_per_block": int(out[1]) // 4,
-                "min_blocks_per_sm": int(out[2])}
+        out = np.zeros(5, np.int32)
+        _check(load().prismq_batch_tuning_ex(self.h, _ptr(out)))
+        return {"variant": int(out[0]), "block": int(out[1]), "atoms_per_block": int(out[3]),
+                "min_blocks_per_sm": int(out[2]), "row_prefetch": int(out[4])}
 
     def atom_span(self) -> int:
         """Length (atoms) of the whole-arena state arrays."""

@@ -1819,6 +1819,18 @@ prismq_status prismq_set_pair_layout(prismq_system* sys, int32_t layout) {
   return prismq_batch_set_pair_layout(sys->b, layout);
 }
 
+prismq_status prismq_batch_tuning_ex(prismq_batch* b, int32_t out[5]) {
+  if (!b || !out) return fail(PRISMQ_E_INVALID, "NULL argument");
+  out[0] = b->force_variant;
+  out[1] = out[2] = out[3] = out[4] = 0;
+  if (b->force_variant >= 0) {
+    force_variant_shape(b->force_variant, &out[1], &out[2]);
+    out[3] = out[1] / kLanes;
+    out[4] = force_variant_prefetch(b->force_variant);
+  }
+  return PRISMQ_OK;
+}
+
 prismq_status prismq_batch_tuning(prismq_batch* b, int32_t out[3]) {
   if (!b || !out) return fail(PRISMQ_E_INVALID, "NULL argument");
   out[0] = b->force_variant;

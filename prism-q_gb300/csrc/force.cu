@@ -541,7 +541,7 @@ __device__ __forceinline__ void force_tiles(const Arena& A, int64_t n_span, int 
 // A block holds kG such groups (128 threads each, consecutive groups); the
 // groups share nothing but the block's barriers, so kG changes the launch
 // shape, never the results.
-template <class R, bool kEnergy, int kMinBlocks, int kG>
+template <class R, bool kEnergy, int kMinBlocks, int kG, int kPf>
 __global__ void __launch_bounds__(128 * kG, kMinBlocks) k_force(Arena A, int64_t n_span, int sel, int cap) {
   // the row builder that ran before this launch consumed the rebuild queue
   // (the branch-B launch of an overlapped step may run beside that builder)
@@ -724,6 +724,13 @@ __global__ void __launch_bounds__(128 * kG, kMinBlocks) k_force(Arena A, int64_t
       R4<R> pj[4];
       R2<R> lj[4];
       if (t + 4 < m4) jn = __ldg(row4 + (int64_t)(t + 4) * 8);
+      // kPf > 0: the row block kPf iterations ahead is requested into L2 now
+      // (inside the lane's own row storage; a prefetch moves no data into
+      // registers and changes no result)
+      if (kPf > 0 && t + 4 * kPf < m4) {
+        const int4* ahead = row4 + (int64_t)(t + 4 * kPf) * 8;
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(ahead));
+      }
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
         pj[u] = ldg_r4(pos + j[u]);
@@ -787,11 +794,15 @@ __global__ void __launch_bounds__(128 * kG, kMinBlocks) k_force(Arena A, int64_t
 // per block (32 or 64: one or two force groups) and the minimum resident
 // blocks per SM handed to the register allocator.  The shape changes neither
 // the per-atom decomposition nor the results.
+// Variants 7-13 repeat 0-6 with the row indices requested into L2 four
+// iterations (16 entries per atom) ahead.
 struct ForceShape {
-  int block, min_blocks;
+  int block, min_blocks, prefetch;
 };
-static const ForceShape kForceShapes[] = {{128, 1}, {128, 8}, {128, 10}, {128, 12},
-                                          {256, 4}, {256, 5}, {256, 6}};
+static const ForceShape kForceShapes[] = {{128, 1, 0}, {128, 8, 0}, {128, 10, 0}, {128, 12, 0},
+                                          {256, 4, 0}, {256, 5, 0}, {256, 6, 0},
+                                          {128, 1, 4}, {128, 8, 4}, {128, 10, 4}, {128, 12, 4},
+                                          {256, 4, 4}, {256, 5, 4}, {256, 6, 4}};
 
 int force_variant_count() { return (int)(sizeof(kForceShapes) / sizeof(kForceShapes[0])); }
 
@@ -800,18 +811,20 @@ void force_variant_shape(int v, int* block, int* min_blocks) {
   *min_blocks = kForceShapes[v].min_blocks;
 }
 
-template <class R, bool kEnergy, int kMinBlocks, int kG = 1>
+int force_variant_prefetch(int v) { return kForceShapes[v].prefetch; }
+
+template <class R, bool kEnergy, int kMinBlocks, int kG = 1, int kPf = 0>
 static void force_launch(const Arena& A, int64_t n, int ob, int cap, cudaStream_t st) {
   const size_t smem = (size_t)kG * cap * (3 * sizeof(R) + (kEnergy ? sizeof(double) : 0));
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_force<R, kEnergy, kMinBlocks, kG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(k_force<R, kEnergy, kMinBlocks, kG, kPf>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)((size_t)kG * kMaxGroupSlots * (3 * sizeof(R) + sizeof(double))));
     attr = true;
   }
   const int64_t groups = (n + kForceGroup - 1) / kForceGroup;
   const unsigned blocks = (unsigned)((groups + kG - 1) / kG);
-  k_force<R, kEnergy, kMinBlocks, kG><<<blocks, 128 * kG, smem, st>>>(A, n, ob, cap);
+  k_force<R, kEnergy, kMinBlocks, kG, kPf><<<blocks, 128 * kG, smem, st>>>(A, n, ob, cap);
 }
 
 void launch_force(const Arena& A, int64_t n_atoms_span, bool energy, cudaStream_t st, int sel, int variant,
@@ -837,6 +850,13 @@ void launch_force(const Arena& A, int64_t n_atoms_span, bool energy, cudaStream_
     case 4: force_launch<float, false, 4, 2>(A, n_atoms_span, ob, cap, st); break;
     case 5: force_launch<float, false, 5, 2>(A, n_atoms_span, ob, cap, st); break;
     case 6: force_launch<float, false, 6, 2>(A, n_atoms_span, ob, cap, st); break;
+    case 7: force_launch<float, false, 1, 1, 4>(A, n_atoms_span, ob, cap, st); break;
+    case 8: force_launch<float, false, 8, 1, 4>(A, n_atoms_span, ob, cap, st); break;
+    case 9: force_launch<float, false, 10, 1, 4>(A, n_atoms_span, ob, cap, st); break;
+    case 10: force_launch<float, false, 12, 1, 4>(A, n_atoms_span, ob, cap, st); break;
+    case 11: force_launch<float, false, 4, 2, 4>(A, n_atoms_span, ob, cap, st); break;
+    case 12: force_launch<float, false, 5, 2, 4>(A, n_atoms_span, ob, cap, st); break;
+    case 13: force_launch<float, false, 6, 2, 4>(A, n_atoms_span, ob, cap, st); break;
     default: force_launch<float, false, 1>(A, n_atoms_span, ob, cap, st); break;
   }
 }

@@ -243,6 +243,7 @@ void launch_force(const Arena& A, int64_t n_atoms_span, bool energy, cudaStream_
                   int sel = kSelAll, int variant = 0, int group_slots = 0);
 int force_variant_count();
 void force_variant_shape(int variant, int* block, int* min_blocks);
+int force_variant_prefetch(int variant);  // row-index L2 prefetch distance (iterations; 0 = none)
 // check64_pass: 0 = systems with FP32 constraint checks, 1 = systems with FP64
 // checks (FP32 batches launch one pass per kind present); FP64 batches ignore it.
 void launch_integrate(const Arena& A, int64_t n_units_span, int mode, cudaStream_t st, int check64_pass = 0);
