@@ -611,11 +611,14 @@ struct GroupShared {
   int run_b[kMaxRuns];        // first sorted-atom index of the run
   int run_off[kMaxRuns + 1];  // exclusive prefix of run lengths
   // cluster-pair tiles of the group: open-addressing table keyed by the
-  // system-local j-cluster + 1 (0 = empty), with the OR of its pair bits
-  int tkey[kTileHash];
-  unsigned tmask[kTileHash];
+  // system-local j-cluster + 1 (0 = empty), with the OR of its pair bits.
+  // The table lives after the warps' GroupShared records and only in
+  // launches for the tile layout (kTileHash keys and masks per warp).
+  int* tkey;
+  unsigned* tmask;
   int tcount;  // keys in the table
 };
+constexpr size_t kTileTableBytes = (size_t)kTileHash * (sizeof(int) + sizeof(unsigned));
 
 // Add pair bits to j-cluster jc_local's entry of the group's tile table.  The
 // table's contents (a set of keys with OR-ed masks) do not depend on the order
@@ -994,6 +997,13 @@ __global__ void __launch_bounds__(kNbrThreads, 3) k_nbr_build(Arena A, int64_t n
   extern __shared__ __align__(16) unsigned char nbr_smem[];
   GroupShared* sh = reinterpret_cast<GroupShared*>(nbr_smem);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+    // a launch for the tile layout carries each warp's table after the records
+    unsigned char* tab = nbr_smem + sizeof(GroupShared) * (kNbrThreads / 32) + warp * kTileTableBytes;
+    sh[warp].tkey = A.pair_layout == 1 ? reinterpret_cast<int*>(tab) : nullptr;
+    sh[warp].tmask = A.pair_layout == 1 ? reinterpret_cast<unsigned*>(tab + kTileHash * sizeof(int)) : nullptr;
+  }
+  __syncwarp();
   const int64_t gw = (int64_t)blockIdx.x * (kNbrThreads / 32) + warp;
   const int64_t n_warps = (int64_t)gridDim.x * (kNbrThreads / 32);
   const int64_t n_groups = A.work_ctl[0];
@@ -1166,14 +1176,18 @@ void launch_control_cells(const Arena& A, int n_sys, int mode, int nbr_override,
 void launch_nbr_build(const Arena& A, int64_t n_atoms_span, int exclude_exceptions, cudaStream_t st,
                       bool persistent) {
   if (n_atoms_span <= 0) return;
-  const size_t smem = sizeof(GroupShared) * (kNbrThreads / 32);
+  // the per-warp tile tables only in launches for the tile layout: a row
+  // build leaves that shared memory to L1
+  const size_t smem_rows = sizeof(GroupShared) * (kNbrThreads / 32);
+  const size_t smem_max = smem_rows + kTileTableBytes * (kNbrThreads / 32);
+  const size_t smem = A.pair_layout == 1 ? smem_max : smem_rows;
   static int resident = 0;  // CTAs that fit on the GPU at once
   if (!resident) {
     int dev = 0, n_sm = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
-    cudaFuncSetAttribute(k_nbr_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_nbr_build, kNbrThreads, smem);
+    cudaFuncSetAttribute(k_nbr_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_nbr_build, kNbrThreads, smem_max);
     resident = std::max(1, n_sm) * std::max(1, per_sm);
   }
   const int64_t groups = (n_atoms_span + 7) / 8;
