@@ -776,7 +776,7 @@ struct prismq_batch {
     if (gexec_tail) cudaGraphExecDestroy(gexec_tail);
     void* ptrs[] = {A.pos, A.vel, A.lj, A.xref, A.f, A.pe, A.atom_sys, A.mask_all, A.mask_ref, A.far,
                     A.far_list, A.inc, A.inc_list, A.ex_idx, A.ex_partner, A.ex_par, A.exc, A.grp, A.grp_refs, A.bonds, A.angles,
-                    A.dihs, A.units, A.unit_order, A.noise, A.nbr, A.nnbr, A.tiles, A.ntile, A.cell_start, A.cell_atoms, A.atom_cell, A.work, A.work_ctl, A.big_list, A.sys,
+                    A.dihs, A.units, A.order_range, A.order_prefix, A.noise, A.nbr, A.nnbr, A.tiles, A.ntile, A.cell_start, A.cell_atoms, A.atom_cell, A.work, A.work_ctl, A.big_list, A.sys,
                     A.pos64, A.vel64, A.f64, A.lj64, d_energy, d_stage, d_stage2, d_stage64};
     for (void* p : ptrs)
       if (p) cudaFree(p);
@@ -797,21 +797,35 @@ struct prismq_batch {
   // so the longest constraint chains start in the first wave of blocks and
   // the short ones fill in behind them.  Each unit is still integrated once,
   // by the same code, so the order changes no result.
-  std::vector<int> h_order;
+  // The order is uploaded as 4 ranges per system slot (a few kB), not as one
+  // index per unit, so admitting or removing a system costs a small copy.
+  std::vector<int2> h_range;
+  std::vector<int> h_prefix;
   int64_t n_order = 0;
   prismq_status upload_order() {
-    h_order.clear();
+    const int nr = 4 * sys_span;
+    h_range.assign((size_t)nr, make_int2(0, 0));
+    h_prefix.assign((size_t)nr + 1, 0);
+    int64_t acc = 0;
+    int k = 0;
     for (int nh = 3; nh >= 0; --nh)
-      for (const SlotRec& R : slots) {
-        if (!R.active) continue;
+      for (int i = 0; i < sys_span; ++i, ++k) {
+        const SlotRec& R = slots[i];
         int64_t b = R.unit_b;
-        for (int k = 3; k > nh; --k) b += R.units_by_nh[3 - k];
-        for (int32_t i = 0; i < R.units_by_nh[3 - nh]; ++i) h_order.push_back((int)(b + i));
+        for (int q = 3; q > nh; --q) b += R.units_by_nh[3 - q];
+        const int cnt = R.active ? R.units_by_nh[3 - nh] : 0;
+        h_range[k] = make_int2((int)b, cnt);
+        h_prefix[k] = (int)acc;
+        acc += cnt;
       }
-    if ((int64_t)h_order.size() != n_order) graph_dirty = true;
-    n_order = (int64_t)h_order.size();
-    if (n_order > 0)
-      PQ_CK(cudaMemcpyAsync(A.unit_order, h_order.data(), sizeof(int) * h_order.size(), cudaMemcpyHostToDevice, st));
+    h_prefix[nr] = (int)acc;
+    if (acc != n_order || nr != A.n_ranges) graph_dirty = true;
+    n_order = acc;
+    A.n_ranges = nr;
+    if (nr > 0) {
+      PQ_CK(cudaMemcpyAsync(A.order_range, h_range.data(), sizeof(int2) * nr, cudaMemcpyHostToDevice, st));
+      PQ_CK(cudaMemcpyAsync(A.order_prefix, h_prefix.data(), sizeof(int) * (nr + 1), cudaMemcpyHostToDevice, st));
+    }
     return PRISMQ_OK;
   }
 
@@ -1251,7 +1265,8 @@ prismq_status batch_alloc(prismq_batch* B, int64_t atom_cap, int sys_cap, int64_
   PQ_ALLOC(A.angles, A.angle_cap);
   PQ_ALLOC(A.dihs, A.dih_cap);
   PQ_ALLOC(A.units, A.unit_cap);
-  PQ_ALLOC(A.unit_order, A.unit_cap);
+  PQ_ALLOC(A.order_range, 4 * (int64_t)sys_cap);
+  PQ_ALLOC(A.order_prefix, 4 * (int64_t)sys_cap + 1);
   PQ_ALLOC(A.noise, 2 * atom_cap);
   PQ_ALLOC(A.nbr, (atom_cap / 32) * (int64_t)kNbrCap * 32);
   PQ_ALLOC(A.nnbr, atom_cap);

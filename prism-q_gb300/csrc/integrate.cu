@@ -15,13 +15,25 @@ namespace pq {
 // R = float: the production step, for the systems whose constraint checks run
 // in FP32 (kCheck64 false) or FP64 (kCheck64 true); R = double: the
 // FP64-everywhere step of an FP64 batch.
-// The grid walks A.unit_order (n_units entries), so the units with the
-// longest constraint chains are scheduled first.
+// The grid walks the batch-wide unit order (n_units entries: the ranges of
+// A.order_range), so the units with the longest constraint chains are
+// scheduled first.
+__device__ __forceinline__ int ordered_unit(const Arena& A, int t) {
+  // the last range whose first walk position is <= t (it is never empty)
+  int lo = 0, hi = A.n_ranges - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(A.order_prefix + mid) <= t) lo = mid;
+    else hi = mid - 1;
+  }
+  return __ldg(&A.order_range[lo].x) + (t - __ldg(A.order_prefix + lo));
+}
+
 template <class R, bool kCheck64>
 __global__ void __launch_bounds__(128, 8) k_integrate(Arena A, int64_t n_units, int mode) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_units) return;
-  const Unit U = A.units[A.unit_order[t]];
+  const Unit U = A.units[ordered_unit(A, (int)t)];
   if (U.nh < 0) return;
   SysDev* Sp = &A.sys[U.sys];
   const SysDev S = *Sp;

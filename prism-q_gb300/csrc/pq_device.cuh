@@ -173,10 +173,14 @@ struct Arena {
   BondT* bonds = nullptr;
   AngleT* angles = nullptr;
   DihT* dihs = nullptr;
-  // constraint units, and the order the integrate grid walks them in
-  // (indices into units: every system's 3-hydrogen units, then 2, 1, 0)
+  // constraint units, and the order the integrate grid walks them in: every
+  // system's 3-hydrogen units, then 2, 1, 0, as ranges of units (range r
+  // holds order_range[r].y units from order_range[r].x; order_prefix[r] is
+  // the walk position of its first unit)
   Unit* units = nullptr;
-  int* unit_order = nullptr;
+  int2* order_range = nullptr;  // [4 * sys_cap]
+  int* order_prefix = nullptr;  // [4 * sys_cap + 1]
+  int n_ranges = 0;
   // OU normals drawn ahead of the integrate launch, per atom: [0, atom_cap)
   // for post(s-1), [atom_cap, 2 atom_cap) for pre(s)
   float4* noise = nullptr;
