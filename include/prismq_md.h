@@ -434,10 +434,8 @@ prismq_status prismq_set_pair_layout(prismq_system* sys, int32_t layout);
  * for 32 atoms, 256 for 64), out[2] = minimum resident blocks per SM given to
  * the register allocator.  The launch shape does not change results. */
 prismq_status prismq_batch_tuning(prismq_batch* b, int32_t out[3]);
-/* The same with out[3] = atoms per block and out[4] = the prefetch mode: its
- * low four bits are how many row-index iterations ahead the kernel asks L2
- * for the atom's row (0: none); bit 0x10 also asks L1 for the next
- * iteration's partner positions and LJ parameters.
+/* The same with out[3] = atoms per block and out[4] = how many row-index
+ * iterations ahead the kernel asks L2 for the atom's row (0: no prefetch).
  * No counterpart in the reference (its launch shape is fixed, one thread per
  * atom, fused_engine.rs:19268-19350). */
 prismq_status prismq_batch_tuning_ex(prismq_batch* b, int32_t out[5]);

@@ -718,31 +718,13 @@ __global__ void __launch_bounds__(128 * kG, kMinBlocks) k_force(Arena A, int64_t
     // every 32 of the lane's entries, as in a loop over 32-entry chunks.
     const int m4 = mine & ~3;
     const int4* row4 = reinterpret_cast<const int4*>(row);  // block t/4 of the lane at row4[32 (t/4)]
-    constexpr int kL2 = kPf & 0xf;           // row block requested into L2 this many iterations ahead
-    constexpr bool kL1 = (kPf & 0x10) != 0;  // next iteration's partners requested into L1
+    constexpr int kL2 = kPf;  // row block requested into L2 this many iterations ahead
     int4 jn = m4 > 0 ? __ldg(row4) : make_int4(0, 0, 0, 0);
-    int4 jn2 = kL1 && m4 > 4 ? __ldg(row4 + 32) : make_int4(0, 0, 0, 0);
     for (int t = 0; t < m4; t += 4) {
       const int j[4] = {jn.x, jn.y, jn.z, jn.w};
       R4<R> pj[4];
       R2<R> lj[4];
-      if constexpr (kL1) {
-        // jn2 (the next four indices) arrived during the previous iteration:
-        // their positions and LJ parameters are requested into L1 now, and
-        // the indices after them start loading
-        if (t + 4 < m4) {
-          const int jj[4] = {jn2.x, jn2.y, jn2.z, jn2.w};
-#pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            asm volatile("prefetch.global.L1 [%0];" ::"l"(pos + jj[u]));
-            asm volatile("prefetch.global.L1 [%0];" ::"l"(ljp + jj[u]));
-          }
-        }
-        jn = jn2;
-        if (t + 8 < m4) jn2 = __ldg(row4 + (int64_t)(t + 8) * 8);
-      } else {
-        if (t + 4 < m4) jn = __ldg(row4 + (int64_t)(t + 4) * 8);
-      }
+      if (t + 4 < m4) jn = __ldg(row4 + (int64_t)(t + 4) * 8);
       // the row block kL2 iterations ahead is requested into L2 now (inside
       // the lane's own row storage; a prefetch moves no data into registers
       // and changes no result)
@@ -813,17 +795,15 @@ __global__ void __launch_bounds__(128 * kG, kMinBlocks) k_force(Arena A, int64_t
 // per block (32 or 64: one or two force groups) and the minimum resident
 // blocks per SM handed to the register allocator.  The shape changes neither
 // the per-atom decomposition nor the results.
-// prefetch: the low four bits are how many iterations ahead the row
-// indices are requested into L2 (0 = none); 0x10 also requests the next
-// iteration's partner positions and LJ parameters into L1.
+// Variants 7-13 repeat 0-6 with the row indices requested into L2 four
+// iterations (16 entries per atom) ahead.
 struct ForceShape {
   int block, min_blocks, prefetch;
 };
 static const ForceShape kForceShapes[] = {{128, 1, 0}, {128, 8, 0}, {128, 10, 0}, {128, 12, 0},
                                           {256, 4, 0}, {256, 5, 0}, {256, 6, 0},
                                           {128, 1, 4}, {128, 8, 4}, {128, 10, 4}, {128, 12, 4},
-                                          {256, 4, 4}, {256, 5, 4}, {256, 6, 4},
-                                          {128, 8, 8}, {128, 8, 0x14}, {128, 10, 0x14}, {256, 4, 0x14}};
+                                          {256, 4, 4}, {256, 5, 4}, {256, 6, 4}};
 
 int force_variant_count() { return (int)(sizeof(kForceShapes) / sizeof(kForceShapes[0])); }
 
@@ -878,10 +858,6 @@ void launch_force(const Arena& A, int64_t n_atoms_span, bool energy, cudaStream_
     case 11: force_launch<float, false, 4, 2, 4>(A, n_atoms_span, ob, cap, st); break;
     case 12: force_launch<float, false, 5, 2, 4>(A, n_atoms_span, ob, cap, st); break;
     case 13: force_launch<float, false, 6, 2, 4>(A, n_atoms_span, ob, cap, st); break;
-    case 14: force_launch<float, false, 8, 1, 8>(A, n_atoms_span, ob, cap, st); break;
-    case 15: force_launch<float, false, 8, 1, 0x14>(A, n_atoms_span, ob, cap, st); break;
-    case 16: force_launch<float, false, 10, 1, 0x14>(A, n_atoms_span, ob, cap, st); break;
-    case 17: force_launch<float, false, 4, 2, 0x14>(A, n_atoms_span, ob, cap, st); break;
     default: force_launch<float, false, 1>(A, n_atoms_span, ob, cap, st); break;
   }
 }
