@@ -466,7 +466,9 @@ prismq_status prismq_batch_set_state_all(prismq_batch* b, const float* xyz, cons
 prismq_status prismq_batch_get_state_all(prismq_batch* b, float* xyz, float* vxyz);
 /* A host-driven step in one call: set_state_all(xyz_in, vxyz_in), n_steps
  * steps, get_state_all(xyz_out, vxyz_out), enqueued back to back with one
- * wait at the end (any array may be NULL; n_steps 0 only transfers).  The
+ * wait at the end (any array may be NULL; n_steps 0 only transfers).  With
+ * a pinned xyz_out the positions are copied back while the last step's forces
+ * and post-force phases still run (those phases move only velocities).  The
  * outputs are filled even when a system fails; the return value is then
  * that failure, as from prismq_batch_step. */
 prismq_status prismq_batch_step_host(prismq_batch* b, int64_t n_steps, const float* xyz_in, const float* vxyz_in,

@@ -767,6 +767,14 @@ struct prismq_batch {
   // latency-bound blocks are scheduled ahead of the force launch's many.
   cudaStream_t st2 = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // Host read-back of a step_host call: positions are final once the last
+  // step's control kernel has run (a COM step's deferred pre-force phases run
+  // there; the post-force phases change velocities only), so the tail graph
+  // records ev_xready after it, and st3 (highest priority) packs the
+  // positions into the staging buffer and copies them to the host by DMA
+  // while the forces and the post-force phases run.
+  cudaStream_t st3 = nullptr;
+  cudaEvent_t ev_xready = nullptr, ev_xdone = nullptr;
 
   ~prismq_batch() {
     for (auto& r : slots)
@@ -782,6 +790,9 @@ struct prismq_batch {
       if (p) cudaFree(p);
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
+    if (ev_xready) cudaEventDestroy(ev_xready);
+    if (ev_xdone) cudaEventDestroy(ev_xdone);
+    if (st3) cudaStreamDestroy(st3);
     if (st2) cudaStreamDestroy(st2);
     if (st) cudaStreamDestroy(st);
   }
@@ -906,10 +917,13 @@ struct prismq_batch {
   // ev (optional, 4 events, captured as external records): before k_decide,
   // after the control kernel, after the row builder, after the join.
   // evb (optional, 2): around the branch-B force launch on st2.
+  // xready (optional, captured as an external record): after the control
+  // kernel, when every position of the step is final.
   // The OU normals of the step's integrate launch (mode) are drawn on st
   // right after the control kernel: they need only the step's decisions, so
   // they run beside the forces instead of after the join.
-  prismq_status enqueue_step_body(int mode, cudaEvent_t* ev = nullptr, cudaEvent_t* evb = nullptr) {
+  prismq_status enqueue_step_body(int mode, cudaEvent_t* ev = nullptr, cudaEvent_t* evb = nullptr,
+                                  cudaEvent_t xready = nullptr) {
     if (ev) PQ_CK(cudaEventRecordWithFlags(ev[0], st, cudaEventRecordExternal));
     launch_decide(A, sys_span, st);
     PQ_CK(cudaEventRecord(ev_fork, st));
@@ -918,6 +932,7 @@ struct prismq_batch {
     launch_force(A, atom_span, false, st2, kSelBranchB, force_variant, group_slots);
     if (evb) PQ_CK(cudaEventRecordWithFlags(evb[1], st2, cudaEventRecordExternal));
     control(kCtlStep, -1, st);
+    if (xready) PQ_CK(cudaEventRecordWithFlags(xready, st, cudaEventRecordExternal));
     launch_noise(A, atom_span, mode, st);
     if (ev) PQ_CK(cudaEventRecordWithFlags(ev[1], st, cudaEventRecordExternal));
     launch_nbr_build(A, atom_span, 1, st, build_persistent);
@@ -976,7 +991,7 @@ struct prismq_batch {
       integrate(kIntPre);
     } else {
       const int mode = part == 1 ? kIntBoth : kIntPost;
-      brc = enqueue_step_body(mode);
+      brc = enqueue_step_body(mode, nullptr, nullptr, part == 2 ? ev_xready : nullptr);
       integrate(mode, false);
     }
     cudaError_t ce = cudaStreamEndCapture(st, &g);
@@ -1235,6 +1250,9 @@ prismq_status batch_alloc(prismq_batch* B, int64_t atom_cap, int sys_cap, int64_
     PQ_CK(cudaStreamCreateWithPriority(&B->st2, cudaStreamNonBlocking, lo));
     PQ_CK(cudaEventCreateWithFlags(&B->ev_fork, cudaEventDisableTiming));
     PQ_CK(cudaEventCreateWithFlags(&B->ev_join, cudaEventDisableTiming));
+    PQ_CK(cudaStreamCreateWithPriority(&B->st3, cudaStreamNonBlocking, hi));
+    PQ_CK(cudaEventCreateWithFlags(&B->ev_xready, cudaEventDisableTiming));
+    PQ_CK(cudaEventCreateWithFlags(&B->ev_xdone, cudaEventDisableTiming));
   }
 #define PQ_ALLOC(ptr, count)                                  \
   do {                                                        \
@@ -2025,7 +2043,23 @@ prismq_status prismq_batch_step_host(prismq_batch* b, int64_t n_steps, const flo
       status_pending = true;
     }
   }
-  if ((rc = enqueue_get_state_all(b, xyz_out, vxyz_out)) != PRISMQ_OK) return rc;
+  if (status_pending && xyz_out && mapped_host(xyz_out)) {
+    // positions on st3 from the tail graph's ev_xready on (packed on the
+    // device, then one DMA copy into the pinned array, beside the last step's
+    // forces), velocities on st after the tail; st then waits for st3
+    const int64_t n = b->atom_span;
+    const unsigned blocks = (unsigned)((n + kStateBlock - 1) / kStateBlock);
+    PQ_CK(cudaStreamWaitEvent(b->st3, b->ev_xready, 0));
+    k_get_state_all<<<blocks, kStateBlock, 0, b->st3>>>(b->A.pos, b->A.vel, b->d_stage, nullptr, n, 1);
+    PQ_CK(cudaMemcpyAsync(xyz_out, b->d_stage, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, b->st3));
+    PQ_CK(cudaEventRecord(b->ev_xdone, b->st3));
+    g_launches += 1;
+    if ((rc = enqueue_get_state_all(b, nullptr, vxyz_out)) != PRISMQ_OK) return rc;
+    PQ_CK(cudaStreamWaitEvent(b->st, b->ev_xdone, 0));
+    PQ_CK(cudaGetLastError());
+  } else if ((rc = enqueue_get_state_all(b, xyz_out, vxyz_out)) != PRISMQ_OK) {
+    return rc;
+  }
   if (status_pending) return b->check_status();  // its read-back waits for the state too
   PQ_CK(cudaStreamSynchronize(b->st));
   return step_rc;

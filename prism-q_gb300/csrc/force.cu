@@ -543,6 +543,10 @@ __device__ __forceinline__ void force_tiles(const Arena& A, int64_t n_span, int 
 // shape, never the results.
 template <class R, bool kEnergy, int kMinBlocks, int kG, int kPf>
 __global__ void __launch_bounds__(128 * kG, kMinBlocks) k_force(Arena A, int64_t n_span, int sel, int cap) {
+  // a pass over the systems the preceding control kernel rebuilt has nothing
+  // to do when the row builder before it found the queue empty (a refresh
+  // after an upload that moved no position)
+  if (sel == kSelRebuilding && A.work_ctl[3] == 0) return;
   // the row builder that ran before this launch consumed the rebuild queue
   // (the branch-B launch of an overlapped step may run beside that builder)
   if (sel != kSelBranchB && blockIdx.x == 0 && threadIdx.x == 0) {

@@ -1007,6 +1007,9 @@ __global__ void __launch_bounds__(kNbrThreads, 3) k_nbr_build(Arena A, int64_t n
   const int64_t gw = (int64_t)blockIdx.x * (kNbrThreads / 32) + warp;
   const int64_t n_warps = (int64_t)gridDim.x * (kNbrThreads / 32);
   const int64_t n_groups = A.work_ctl[0];
+  // the queue length, kept for the force launch that follows (which clears
+  // work_ctl[0] as it starts)
+  if (blockIdx.x == 0 && threadIdx.x == 0) A.work_ctl[3] = (int)n_groups;
   for (int64_t v = gw; v < n_groups; v += n_warps) {
     const int64_t g = A.work[v];
     if (g * 8 >= n_span) continue;

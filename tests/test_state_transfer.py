@@ -126,3 +126,34 @@ def test_step_host_equals_upload_step_download(gpu, topos, form):
     assert np.array_equal(xo, xr) and np.array_equal(vo, vr)
     a.close()
     b.close()
+
+
+def test_step_host_read_back_on_com_steps(gpu, topos):
+    """The pinned read-back of step_host takes the positions while the last
+    step's forces run; on a COM step the deferred pre-force phases move the
+    positions inside the control kernel, so those calls must still return the
+    final positions (COM removal every second step, calls of 1-3 steps)."""
+    def batch():
+        b = gpu.Batch(max_atoms=4096, max_systems=4)
+        for k, t in enumerate(topos):
+            b.add_system(t, gpu.Params(stream=k, com_interval=2))
+        b.step(5)
+        return b
+
+    a, b = batch(), batch()
+    span = a.atom_span()
+    x, v = a.get_state_all()
+    tx, px = _pinned(3 * span)
+    tv, pv = _pinned(3 * span)
+    px[:] = x
+    pv[:] = v
+    xr, vr = x.copy(), v.copy()
+    for n in (1, 2, 3, 1, 1, 2):
+        a.step_host(n, px, pv, px, pv)
+        b.set_state_all(xr, vr)
+        b.step(n)
+        b.get_state_all(xr, vr)
+        assert np.array_equal(px, xr) and np.array_equal(pv, vr)
+    del tx, tv
+    a.close()
+    b.close()
