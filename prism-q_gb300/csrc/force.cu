@@ -221,6 +221,21 @@ __device__ __forceinline__ R pair_scalar(R r2, R sig, R eps, R qq, R& inv_r, R& 
   return fma_r(R(24.0f) * eps * inv_r2, u, fc);        // 24 eps/r^2 (2 s6^2 - s6) + qq k/r^3
 }
 
+// The same law for an ordinary pair with atom i's factors taken out of the
+// pair: kqi = 332.0636·q_i and e24i = 24·√ε_i (LJ parameters hold √ε), so
+// the pair costs three multiplications fewer:
+// fs = (24 ε (2 s6² − s6) + k q_i q_j / r) / r², with s6 = (σ/r)^6.
+template <class R>
+__device__ __forceinline__ R pair_fs(R r2, R sig, R e24i, R sqrt_eps_j, R kqi, R qj, R& inv_r, R& s6) {
+  inv_r = inv_sqrt_r(r2);
+  const R inv_r2 = inv_r * inv_r;
+  const R s2 = sig * sig * inv_r2;
+  s6 = s2 * s2 * s2;
+  const R u = s6 * fma_r(R(2.0f), s6, R(-1.0f));  // 2 s6^2 - s6
+  const R cr = kqi * qj * inv_r;
+  return fma_r(e24i * sqrt_eps_j, u, cr) * inv_r2;
+}
+
 // f -= fs * d, one rounding per component.
 template <class R>
 __device__ __forceinline__ void acc_pair(Acc<R>& f, R fs, R dx, R dy, R dz) {
@@ -245,14 +260,13 @@ __device__ __forceinline__ double lane_sum(double v) {
 // One ordinary pair, branch-free: force on i from j when r^2 lies in
 // [0.01, cutoff^2), an exact zero otherwise.
 template <class R>
-__device__ __forceinline__ void pair_accumulate(const R4<R> pi, R qi, R2<R> li, const R4<R> pj, R2<R> lj, R cut2,
-                                                Acc<R>& f) {
+__device__ __forceinline__ void pair_accumulate(const R4<R> pi, R kqi, R sig_i, R e24i, const R4<R> pj, R2<R> lj,
+                                                R cut2, Acc<R>& f) {
   const R dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
   const R r2 = fma_r(dz, dz, fma_r(dy, dy, dx * dx));
   const bool in = r2 < cut2 && r2 >= R(kMinPairR2);
-  const R sig = li.x + lj.x, eps = li.y * lj.y, qq = qi * pj.w;
   R inv_r, s6;
-  R fs = pair_scalar<R>(max_r(r2, R(kMinPairR2)), sig, eps, qq, inv_r, s6);
+  R fs = pair_fs<R>(max_r(r2, R(kMinPairR2)), sig_i + lj.x, e24i, lj.y, kqi, pj.w, inv_r, s6);
   fs = in ? fs : R(0.0f);
   acc_pair<R>(f, fs, dx, dy, dz);
 }
@@ -706,6 +720,7 @@ __global__ void __launch_bounds__(128 * kG, kMinBlocks) k_force(Arena A, int64_t
   const R2<R>* ljp = lj_params(A, R(0));
   const R2<R> li = ljp[a];
   const R qi = pi.w;
+  const R kqi = R(kCoulomb) * qi, e24i = R(24.0f) * li.y;
   const int n = A.nnbr[a];
   const int* row = A.nbr + nbr_index(a, q);  // entry 4t+q is at row[128 (t/4) + t%4]
   R inv_rc = R(0.0f);
@@ -742,12 +757,12 @@ __global__ void __launch_bounds__(128 * kG, kMinBlocks) k_force(Arena A, int64_t
         lj[u] = __ldg(ljp + j[u]);
       }
 #pragma unroll
-      for (int u = 0; u < 4; ++u) pair_accumulate<R>(pi, qi, li, pj[u], lj[u], cut2, f);
+      for (int u = 0; u < 4; ++u) pair_accumulate<R>(pi, kqi, li.x, e24i, pj[u], lj[u], cut2, f);
       if (((t + 4) & 31) == 0) f.flush();
     }
     for (int t = m4; t < mine; ++t) {
       const int j = __ldg(row + (int64_t)(t >> 2) * 128 + (t & 3));
-      pair_accumulate<R>(pi, qi, li, ldg_r4(pos + j), __ldg(ljp + j), cut2, f);
+      pair_accumulate<R>(pi, kqi, li.x, e24i, ldg_r4(pos + j), __ldg(ljp + j), cut2, f);
     }
     f.flush();
   } else
@@ -763,7 +778,7 @@ __global__ void __launch_bounds__(128 * kG, kMinBlocks) k_force(Arena A, int64_t
           const R2<R> lj = __ldg(ljp + j);
           const R sig = li.x + lj.x, eps = li.y * lj.y, qq = qi * pj.w;
           R inv_r, s6;
-          const R fs = pair_scalar<R>(r2, sig, eps, qq, inv_r, s6);
+          const R fs = pair_fs<R>(r2, sig, e24i, lj.y, kqi, pj.w, inv_r, s6);
           acc_pair<R>(f, fs, dx, dy, dz);
           if (kEnergy) {
             const R sc2 = sig * sig * inv_rc * inv_rc;
