@@ -19,7 +19,10 @@
 //   * partial sums are FP32 over at most 32 pairs and then accumulated in
 //     int64 fixed point at 2^-32 kcal/mol/Å, so the force of an atom is a
 //     deterministic function of its own row alone;
-//   * energies are computed only by the energy variant (FP64 per-atom planes).
+//   * energies are computed only by the energy variant (FP64 per-atom planes);
+//   * the file is compiled without FMA contraction (the pair law's FMAs are
+//     written out) and with subnormals flushed to zero, which changes no
+//     IEEE-rounded result on normal values.
 //
 // The kernel is a template over the real type R.  R = float is the production
 // path above.  R = double is the FP64-everywhere run of the precision study:
@@ -266,7 +269,9 @@ __device__ __forceinline__ void pair_accumulate(const R4<R> pi, R kqi, R sig_i, 
   const R r2 = fma_r(dz, dz, fma_r(dy, dy, dx * dx));
   const bool in = r2 < cut2 && r2 >= R(kMinPairR2);
   R inv_r, s6;
-  R fs = pair_fs<R>(max_r(r2, R(kMinPairR2)), sig_i + lj.x, e24i, lj.y, kqi, pj.w, inv_r, s6);
+  // outside [0.01, cutoff^2) the law may overflow or divide by zero; the
+  // select below discards that value
+  R fs = pair_fs<R>(r2, sig_i + lj.x, e24i, lj.y, kqi, pj.w, inv_r, s6);
   fs = in ? fs : R(0.0f);
   acc_pair<R>(f, fs, dx, dy, dz);
 }
