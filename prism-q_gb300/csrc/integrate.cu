@@ -10,8 +10,10 @@
 namespace pq {
 
 // One thread per constraint unit.  The OU normals arrive drawn (k_noise), and
-// eight resident blocks per SM (64 registers) trade a few spilled words for
-// 1.4x the occupancy of the unconstrained 91-register build.
+// six resident blocks per SM (80 registers, a few spilled words) are the
+// measured balance between occupancy and spills: on the 256-system workload
+// the launch takes 0.074 ms against 0.086 ms at eight blocks (64 registers)
+// and 0.085 ms at four (102 registers, no spills).
 // R = float: the production step, for the systems whose constraint checks run
 // in FP32 (kCheck64 false) or FP64 (kCheck64 true); R = double: the
 // FP64-everywhere step of an FP64 batch.
@@ -30,7 +32,7 @@ __device__ __forceinline__ int ordered_unit(const Arena& A, int t) {
 }
 
 template <class R, bool kCheck64>
-__global__ void __launch_bounds__(128, 8) k_integrate(Arena A, int64_t n_units, int mode) {
+__global__ void __launch_bounds__(128, 6) k_integrate(Arena A, int64_t n_units, int mode) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_units) return;
   const Unit U = A.units[ordered_unit(A, (int)t)];
