@@ -571,6 +571,7 @@ __global__ void __launch_bounds__(128 * kG, kMinBlocks) k_force(Arena A, int64_t
   if (sel != kSelBranchB && blockIdx.x == 0 && threadIdx.x == 0) {
     A.work_ctl[0] = 0;
     A.work_ctl[1] = 0;
+    A.work_ctl[2] = 0;
   }
   extern __shared__ __align__(16) unsigned char force_smem[];
   __shared__ int s_base_g[kG][kForceGroup], s_nb_g[kG][kForceGroup], s_na_g[kG][kForceGroup],

@@ -14,11 +14,12 @@
 //                    that rows come out in a deterministic order without a
 //                    per-row sort.  It then queues the 8-atom groups of every
 //                    rebuilding system on a device work list.
-//   k_nbr_build      one warp per queued 8-atom group (a persistent grid of
-//                    the resident CTAs when it runs beside the forces of a
-//                    many-system step, every group's warp at once when it
-//                    runs alone).  The warp lists the cell-row runs of the
-//                    union of its atoms' stencils (the x-run of cells in one
+//   k_nbr_build      one warp per queued 8-atom group at a time (a grid of
+//                    the resident CTAs; round-robin over the queue when it
+//                    runs beside the forces of a many-system step, from a
+//                    shared counter when it runs alone).  The warp lists the
+//                    cell-row runs of the union of its atoms' stencils (the
+//                    x-run of cells in one
 //                    (y, z) row is one contiguous run of sorted atoms), streams
 //                    their candidates in full 32-lane chunks, tests each
 //                    against the eight atoms, applies the exclusion window
@@ -989,11 +990,14 @@ __device__ __forceinline__ void build_group(const Arena& A, int64_t g, int exclu
   __syncwarp();
 }
 
-// Warps walk the queued 8-atom groups round-robin (no shared counter, no
-// atomics); the force kernel that follows in the same stream clears the
-// queue.  Complete lists are built a group at a time; REF27 lists (parity
+// Warps walk the queued 8-atom groups round-robin (`dynamic` 0), or take
+// them one at a time from a shared counter (work_ctl[2], `dynamic` 1), so
+// that a warp that drew cheap groups takes more of them; which warp builds a
+// group does not change its rows.  The force kernel that follows in the same
+// stream clears the queue and the counter.  Complete lists are built a group at a time; REF27 lists (parity
 // only) atom by atom with the reference's own 27-cell stencil.
-__global__ void __launch_bounds__(kNbrThreads, 3) k_nbr_build(Arena A, int64_t n_span, int exclude_exc) {
+__global__ void __launch_bounds__(kNbrThreads, 3) k_nbr_build(Arena A, int64_t n_span, int exclude_exc,
+                                                              int dynamic) {
   extern __shared__ __align__(16) unsigned char nbr_smem[];
   GroupShared* sh = reinterpret_cast<GroupShared*>(nbr_smem);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1010,8 +1014,16 @@ __global__ void __launch_bounds__(kNbrThreads, 3) k_nbr_build(Arena A, int64_t n
   // the queue length, kept for the force launch that follows (which clears
   // work_ctl[0] as it starts)
   if (blockIdx.x == 0 && threadIdx.x == 0) A.work_ctl[3] = (int)n_groups;
-  for (int64_t v = gw; v < n_groups; v += n_warps) {
+  if (gw >= n_groups) return;  // warps beyond the queue length leave at once
+  for (int64_t v = gw;;) {
+    if (dynamic) {
+      int t = 0;
+      if (lane == 0) t = atomicAdd(&A.work_ctl[2], 1);
+      v = __shfl_sync(0xffffffffu, t, 0);
+    }
+    if (v >= n_groups) break;
     const int64_t g = A.work[v];
+    if (!dynamic) v += n_warps;
     if (g * 8 >= n_span) continue;
     const int s = A.atom_sys[g * 8];
     if (s >= 0 && A.sys[s].nbr_mode == 1) {
@@ -1169,13 +1181,15 @@ void launch_control_cells(const Arena& A, int n_sys, int mode, int nbr_override,
   k_control_cells<<<n_sys, kCtlThreads, smem, st>>>(A, mode, nbr_override);
 }
 
-// Grid: with `persistent`, the CTAs that fit on the GPU at once, whose warps
-// stride over the queued groups; otherwise one warp per possible group (CTAs
-// past the queue leave at once).  The persistent grid holds the SMs' registers
-// for the whole build, which suits a builder that runs beside the overlapped
-// force launch of a many-system step; a builder that runs alone (priming, or
-// a step of one or two systems, where a rebuild has nothing to overlap)
-// finishes sooner with every group's warp in flight.
+// Grid: the CTAs that fit on the GPU at once (fewer for a short span).  With
+// `persistent` (a builder beside the overlapped force launch of a
+// many-system step) the warps stride over the queue round-robin; otherwise
+// (priming, or a step of one or two systems, where a rebuild has nothing to
+// overlap) they take groups from the shared counter, which on the
+// 100,000-atom system took the builder from 0.184 to 0.172 ms per step
+// against one warp per group.  The counter is no help beside the force
+// launch: the builder then finishes sooner but takes more of the GPU from it
+// (256 systems: 0.877 against 0.868 ms per step).
 void launch_nbr_build(const Arena& A, int64_t n_atoms_span, int exclude_exceptions, cudaStream_t st,
                       bool persistent) {
   if (n_atoms_span <= 0) return;
@@ -1195,8 +1209,8 @@ void launch_nbr_build(const Arena& A, int64_t n_atoms_span, int exclude_exceptio
   }
   const int64_t groups = (n_atoms_span + 7) / 8;
   const int64_t per_group = (groups + kNbrThreads / 32 - 1) / (kNbrThreads / 32);
-  const int grid = (int)(persistent ? std::min<int64_t>(groups, resident) : std::min<int64_t>(per_group, 1 << 30));
-  k_nbr_build<<<grid, kNbrThreads, smem, st>>>(A, n_atoms_span, exclude_exceptions);
+  const int grid = (int)std::min<int64_t>(per_group, resident);
+  k_nbr_build<<<grid, kNbrThreads, smem, st>>>(A, n_atoms_span, exclude_exceptions, persistent ? 0 : 1);
 }
 
 }  // namespace pq
