@@ -840,9 +840,10 @@ struct prismq_batch {
     return PRISMQ_OK;
   }
 
-  // The step's row builder keeps a persistent grid once more than two
-  // systems are resident (it then runs beside the other systems' forces).
-  bool build_persistent = false;
+  // The step's row builder walks its queue round-robin once more than two
+  // systems are resident (it then runs beside the other systems' forces);
+  // otherwise its warps take groups from a shared counter.
+  bool build_round_robin = false;
 
   void update_spans() {
     const int64_t na = r_atoms.high(), nu = r_units.high();
@@ -865,8 +866,8 @@ struct prismq_batch {
     if ((c32 > 0) != (n_check32 > 0) || (c64 > 0) != (n_check64 > 0)) graph_dirty = true;
     int resident = 0;
     for (const SlotRec& R : slots) resident += R.active ? 1 : 0;
-    if ((resident > 2) != build_persistent) graph_dirty = true;
-    build_persistent = resident > 2;
+    if ((resident > 2) != build_round_robin) graph_dirty = true;
+    build_round_robin = resident > 2;
     n_check32 = c32;
     n_check64 = c64;
     atom_span = na;
@@ -935,7 +936,7 @@ struct prismq_batch {
     if (xready) PQ_CK(cudaEventRecordWithFlags(xready, st, cudaEventRecordExternal));
     launch_noise(A, atom_span, mode, st);
     if (ev) PQ_CK(cudaEventRecordWithFlags(ev[1], st, cudaEventRecordExternal));
-    launch_nbr_build(A, atom_span, 1, st, build_persistent);
+    launch_nbr_build(A, atom_span, 1, st, build_round_robin);
     if (ev) PQ_CK(cudaEventRecordWithFlags(ev[2], st, cudaEventRecordExternal));
     launch_force(A, atom_span, false, st, kSelBranchA, force_variant, group_slots);
     PQ_CK(cudaEventRecord(ev_join, st2));

@@ -1182,7 +1182,7 @@ void launch_control_cells(const Arena& A, int n_sys, int mode, int nbr_override,
 }
 
 // Grid: the CTAs that fit on the GPU at once (fewer for a short span).  With
-// `persistent` (a builder beside the overlapped force launch of a
+// `round_robin` (a builder beside the overlapped force launch of a
 // many-system step) the warps stride over the queue round-robin; otherwise
 // (priming, or a step of one or two systems, where a rebuild has nothing to
 // overlap) they take groups from the shared counter, which on the
@@ -1191,7 +1191,7 @@ void launch_control_cells(const Arena& A, int n_sys, int mode, int nbr_override,
 // launch: the builder then finishes sooner but takes more of the GPU from it
 // (256 systems: 0.877 against 0.868 ms per step).
 void launch_nbr_build(const Arena& A, int64_t n_atoms_span, int exclude_exceptions, cudaStream_t st,
-                      bool persistent) {
+                      bool round_robin) {
   if (n_atoms_span <= 0) return;
   // the per-warp tile tables only in launches for the tile layout: a row
   // build leaves that shared memory to L1
@@ -1210,7 +1210,7 @@ void launch_nbr_build(const Arena& A, int64_t n_atoms_span, int exclude_exceptio
   const int64_t groups = (n_atoms_span + 7) / 8;
   const int64_t per_group = (groups + kNbrThreads / 32 - 1) / (kNbrThreads / 32);
   const int grid = (int)std::min<int64_t>(per_group, resident);
-  k_nbr_build<<<grid, kNbrThreads, smem, st>>>(A, n_atoms_span, exclude_exceptions, persistent ? 0 : 1);
+  k_nbr_build<<<grid, kNbrThreads, smem, st>>>(A, n_atoms_span, exclude_exceptions, round_robin ? 0 : 1);
 }
 
 }  // namespace pq

@@ -238,7 +238,7 @@ void launch_decide(const Arena& A, int n_sys, cudaStream_t st);
 // Force launch selections.
 constexpr int kSelAll = 0, kSelRebuilding = 1, kSelBranchA = 2, kSelBranchB = 3;
 void launch_nbr_build(const Arena& A, int64_t n_atoms_span, int exclude_exceptions,
-                      cudaStream_t st, bool persistent = false);
+                      cudaStream_t st, bool round_robin = false);
 // group_slots: the largest number of bonded + exception incidences of one
 // 32-atom group among the resident systems (sizes the shared-memory slots).
 // sel: kSelAll, kSelRebuilding (systems rebuilt by the preceding control
