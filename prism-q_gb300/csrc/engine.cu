@@ -235,6 +235,7 @@ prismq_status lower_topology(const prismq_topology* T, Lowered* L) {
     if (!in_range(d.i) || !in_range(d.j) || !in_range(d.k) || !in_range(d.l))
       return fail(PRISMQ_E_INVALID, "dihedral " + std::to_string(t) + " has invalid atoms");
     L->dihs.push_back({d.i, d.j, d.k, d.l, d.periodicity, d.phase, d.force_k,
+                       (float)std::cos((double)d.phase), (float)std::sin((double)d.phase),
                        ((int)id[d.i].size() & 255) | (((int)id[d.j].size() & 255) << 8) |
                            (((int)id[d.k].size() & 255) << 16) | (((int)id[d.l].size() & 255) << 24)});
     id[d.i].push_back(t * 4 + 0);

@@ -79,10 +79,6 @@ __device__ __forceinline__ float sqrt_r(float x) { return sqrtf(x); }
 __device__ __forceinline__ double sqrt_r(double x) { return sqrt(x); }
 __device__ __forceinline__ float acos_r(float x) { return acosf(x); }
 __device__ __forceinline__ double acos_r(double x) { return acos(x); }
-__device__ __forceinline__ float asin_r(float x) { return asinf(x); }
-__device__ __forceinline__ double asin_r(double x) { return asin(x); }
-__device__ __forceinline__ float sin_r(float x) { return sinf(x); }
-__device__ __forceinline__ double sin_r(double x) { return sin(x); }
 __device__ __forceinline__ float inv_sqrt_r(float x) { return rsqrtf(x); }
 __device__ __forceinline__ double inv_sqrt_r(double x) { return 1.0 / sqrt(x); }
 __device__ __forceinline__ float fma_r(float a, float b, float c) { return fmaf(a, b, c); }
@@ -112,102 +108,6 @@ struct Acc<double> {
   double x, y, z;
   __device__ __forceinline__ void flush() {}
 };
-
-// ---- bonded laws ----
-
-template <class R>
-__device__ __forceinline__ void bond_term(const R4<R>* pos, const BondT b, int p, Acc<R>& f, double* e) {
-  const R4<R> pi = pos[b.i], pj = pos[b.j];
-  const R rx = pj.x - pi.x, ry = pj.y - pi.y, rz = pj.z - pi.z;
-  const R r = sqrt_r(rx * rx + ry * ry + rz * rz);
-  if (r < R(1e-8f)) return;
-  const R dr = r - R(b.r0);
-  const R fm = R(-2.0f) * R(b.k) * dr / r;
-  const R s = p == 0 ? -fm : fm;  // fi -= f, fj += f
-  f.x += s * rx;
-  f.y += s * ry;
-  f.z += s * rz;
-  if (e) *e += (double)b.k * (double)dr * (double)dr * 0.5;
-}
-
-template <class R>
-__device__ __forceinline__ void angle_term(const R4<R>* pos, const AngleT a, int p, Acc<R>& f, double* e) {
-  const R4<R> pi = pos[a.i], pj = pos[a.j], pk = pos[a.k];
-  const R ax = pi.x - pj.x, ay = pi.y - pj.y, az = pi.z - pj.z;  // rij
-  const R bx = pk.x - pj.x, by = pk.y - pj.y, bz = pk.z - pj.z;  // rkj
-  const R la = sqrt_r(ax * ax + ay * ay + az * az);
-  const R lb = sqrt_r(bx * bx + by * by + bz * bz);
-  if (la < R(1e-8f) || lb < R(1e-8f)) return;
-  R c = (ax * bx + ay * by + az * bz) / (la * lb);
-  c = max_r(R(-1.0f), min_r(R(1.0f), c));
-  const R th = acos_r(c);
-  const R dth = th - R(a.theta0);
-  R sn = sqrt_r(R(1.0f) - c * c);
-  if (sn < R(1e-8f)) sn = R(1e-8f);
-  const R fm = R(-2.0f) * R(a.kf) * dth / sn;
-  const R ia = R(1.0f) / la, ib = R(1.0f) / lb;
-  const R dix = (bx * ib - c * ax * ia) * ia, diy = (by * ib - c * ay * ia) * ia, diz = (bz * ib - c * az * ia) * ia;
-  const R dkx = (ax * ia - c * bx * ib) * ib, dky = (ay * ia - c * by * ib) * ib, dkz = (az * ia - c * bz * ib) * ib;
-  if (p == 0) {
-    f.x -= fm * dix;
-    f.y -= fm * diy;
-    f.z -= fm * diz;
-  } else if (p == 2) {
-    f.x -= fm * dkx;
-    f.y -= fm * dky;
-    f.z -= fm * dkz;
-  } else {
-    f.x += fm * (dix + dkx);
-    f.y += fm * (diy + dky);
-    f.z += fm * (diz + dkz);
-  }
-  if (e) *e += (double)a.kf * (double)dth * (double)dth * (1.0 / 3.0);
-}
-
-template <class R>
-__device__ __forceinline__ void dihedral_term(const R4<R>* pos, const DihT d, int p, Acc<R>& f, double* e) {
-  const R4<R> pi = pos[d.i], pj = pos[d.j], pk = pos[d.k], pl = pos[d.l];
-  const R v0x = pi.x - pj.x, v0y = pi.y - pj.y, v0z = pi.z - pj.z;
-  const R v1x = pk.x - pj.x, v1y = pk.y - pj.y, v1z = pk.z - pj.z;
-  const R v2x = pk.x - pl.x, v2y = pk.y - pl.y, v2z = pk.z - pl.z;
-  const R c0x = v0y * v1z - v0z * v1y, c0y = v0z * v1x - v0x * v1z, c0z = v0x * v1y - v0y * v1x;
-  const R c1x = v1y * v2z - v1z * v2y, c1y = v1z * v2x - v1x * v2z, c1z = v1x * v2y - v1y * v2x;
-  const R n1 = c0x * c0x + c0y * c0y + c0z * c0z;
-  const R n2 = c1x * c1x + c1y * c1y + c1z * c1z;
-  const R nb = v1x * v1x + v1y * v1y + v1z * v1z;
-  if (n1 < R(1e-16f) || n2 < R(1e-16f) || nb < R(1e-16f)) return;
-  const R lbc = sqrt_r(nb);
-  R cp = (c0x * c1x + c0y * c1y + c0z * c1z) / sqrt_r(n1 * n2);
-  cp = max_r(R(-1.0f), min_r(R(1.0f), cp));
-  R phi;
-  if (cp > R(0.99f) || cp < R(-0.99f)) {
-    const R xx = c0y * c1z - c0z * c1y, xy = c0z * c1x - c0x * c1z, xz = c0x * c1y - c0y * c1x;
-    R s2 = (xx * xx + xy * xy + xz * xz) / (n1 * n2);
-    s2 = max_r(R(0.0f), min_r(R(1.0f), s2));
-    phi = asin_r(sqrt_r(s2));
-    if (cp < R(0.0f)) phi = R(3.14159265358979323846) - phi;
-  } else {
-    phi = acos_r(cp);
-  }
-  if (v0x * c1x + v0y * c1y + v0z * c1z < R(0.0f)) phi = -phi;
-  const R n = (R)d.n;
-  const R dE = -R(d.kf) * n * sin_r(n * phi - R(d.phase));
-  const R inb = R(1.0f) / nb;
-  const R ff0 = (-dE * lbc) / n1;
-  const R ff1 = (v0x * v1x + v0y * v1y + v0z * v1z) * inb;
-  const R ff2 = (v2x * v1x + v2y * v1y + v2z * v1z) * inb;
-  const R ff3 = (dE * lbc) / n2;
-  const R f1x = ff0 * c0x, f1y = ff0 * c0y, f1z = ff0 * c0z;
-  const R f4x = ff3 * c1x, f4y = ff3 * c1y, f4z = ff3 * c1z;
-  const R sx = ff1 * f1x - ff2 * f4x, sy = ff1 * f1y - ff2 * f4y, sz = ff1 * f1z - ff2 * f4z;
-  switch (p) {
-    case 0: f.x += f1x; f.y += f1y; f.z += f1z; break;
-    case 1: f.x += sx - f1x; f.y += sy - f1y; f.z += sz - f1z; break;
-    case 2: f.x += -sx - f4x; f.y += -sy - f4y; f.z += -sz - f4z; break;
-    default: f.x += f4x; f.y += f4y; f.z += f4z; break;
-  }
-  if (e) *e += (double)d.kf * (1.0 + cos((double)n * (double)phi - (double)d.phase)) * 0.25;
-}
 
 // ---- pair law: force on i from j (d = xj - xi), LJ + Coulomb ----
 // The file is compiled without FMA contraction, so every fused multiply-add
@@ -298,10 +198,11 @@ __device__ __forceinline__ void store_force(const Arena& A, int a, const Acc<dou
 // ---- per-term contributions, as each member's gather adds them ----
 //
 // A term is evaluated once; member m's contribution is the value the member
-// would add to its own force (the per-member laws above: bond s*r with
-// s = -fm or fm, angle -(fm*d) for the ends and fm*(di+dk) for the apex,
-// torsion f1, s-f1, -s-f4, f4; exceptions -(fs*d) seen from either member,
-// d = x_partner - x_self, which is the same number negated).
+// would add to its own force if it evaluated the term itself: for a bond
+// -fm*r and +fm*r (r = x_j - x_i, fm = -2k(r - r0)/r), for an angle -(fm*d)
+// at the ends and fm*(d_i + d_k) at the apex, for a torsion f1, s - f1,
+// -s - f4 and f4 (the OpenMM torsion gradient), for an exception -(fs*d)
+// seen from either member (d = x_partner - x_self, the same number negated).
 template <class R>
 struct TermOut {
   R x[4], y[4], z[4];
@@ -348,6 +249,15 @@ __device__ __forceinline__ bool angle_out(const R4<R>* pos, const AngleT a, Term
   return true;
 }
 
+// Periodic torsion U = k (1 + cos(n phi - delta)) / 4 with the OpenMM
+// gradient (compute_dihedral_force, nhs_amber_fused.cu:525).  phi is not
+// formed: cos phi = c0.c1 / (|c0||c1|) and, because c0 x c1 = v1 (v0.c1),
+// sin phi = |v1| (v0.c1) / (|c0||c1|) with the reference's sign (phi < 0
+// when v0.c1 < 0); cos and sin of n phi follow by the angle-addition
+// recurrence and sin(n phi - delta) = sin(n phi) cos(delta) - cos(n phi)
+// sin(delta) from cos(delta), sin(delta) computed once per term on the host.
+// The reference takes phi through acosf/asinf and then sinf; the two agree to
+// FP32 rounding.
 template <class R>
 __device__ __forceinline__ bool dihedral_out(const R4<R>* pos, const DihT d, TermOut<R>& o) {
   const R4<R> pi = pos[d.i], pj = pos[d.j], pk = pos[d.k], pl = pos[d.l];
@@ -361,21 +271,22 @@ __device__ __forceinline__ bool dihedral_out(const R4<R>* pos, const DihT d, Ter
   const R nb = v1x * v1x + v1y * v1y + v1z * v1z;
   if (n1 < R(1e-16f) || n2 < R(1e-16f) || nb < R(1e-16f)) return false;
   const R lbc = sqrt_r(nb);
-  R cp = (c0x * c1x + c0y * c1y + c0z * c1z) / sqrt_r(n1 * n2);
+  const R inv_n12 = R(1.0f) / sqrt_r(n1 * n2);
+  R cp = (c0x * c1x + c0y * c1y + c0z * c1z) * inv_n12;
+  R sp = lbc * (v0x * c1x + v0y * c1y + v0z * c1z) * inv_n12;
   cp = max_r(R(-1.0f), min_r(R(1.0f), cp));
-  R phi;
-  if (cp > R(0.99f) || cp < R(-0.99f)) {
-    const R xx = c0y * c1z - c0z * c1y, xy = c0z * c1x - c0x * c1z, xz = c0x * c1y - c0y * c1x;
-    R s2 = (xx * xx + xy * xy + xz * xz) / (n1 * n2);
-    s2 = max_r(R(0.0f), min_r(R(1.0f), s2));
-    phi = asin_r(sqrt_r(s2));
-    if (cp < R(0.0f)) phi = R(3.14159265358979323846) - phi;
-  } else {
-    phi = acos_r(cp);
+  sp = max_r(R(-1.0f), min_r(R(1.0f), sp));
+  // cos and sin of n phi (n < 0: sin changes sign)
+  const int n_abs = d.n < 0 ? -d.n : d.n;
+  const R spn = d.n < 0 ? -sp : sp;
+  R cn = R(1.0f), sn = R(0.0f);
+  for (int k = 0; k < n_abs; ++k) {
+    const R c2 = cn * cp - sn * spn;
+    sn = sn * cp + cn * spn;
+    cn = c2;
   }
-  if (v0x * c1x + v0y * c1y + v0z * c1z < R(0.0f)) phi = -phi;
   const R n = (R)d.n;
-  const R dE = -R(d.kf) * n * sin_r(n * phi - R(d.phase));
+  const R dE = -R(d.kf) * n * (sn * R(d.cos_ph) - cn * R(d.sin_ph));
   const R inb = R(1.0f) / nb;
   const R ff0 = (-dE * lbc) / n1;
   const R ff1 = (v0x * v1x + v0y * v1y + v0z * v1z) * inb;
@@ -388,7 +299,7 @@ __device__ __forceinline__ bool dihedral_out(const R4<R>* pos, const DihT d, Ter
   o.x[1] = sx - f1x; o.y[1] = sy - f1y; o.z[1] = sz - f1z;
   o.x[2] = -sx - f4x; o.y[2] = -sy - f4y; o.z[2] = -sz - f4z;
   o.x[3] = f4x; o.y[3] = f4y; o.z[3] = f4z;
-  o.e = (double)d.kf * (1.0 + cos((double)n * (double)phi - (double)d.phase)) * 0.25;
+  o.e = (double)d.kf * (1.0 + ((double)cn * (double)d.cos_ph + (double)sn * (double)d.sin_ph)) * 0.25;
   return true;
 }
 

@@ -60,6 +60,7 @@ struct DihT {
   int i, j, k, l;
   int n;
   float phase, kf;
+  float cos_ph, sin_ph;  // cos and sin of the phase, from the host in double
   int pos;  // 8 bits per member
 };
 // One exact 1-4 exception pair (each pair once), with its rank in each
