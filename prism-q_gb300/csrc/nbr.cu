@@ -19,8 +19,8 @@
 //                    runs beside the forces of a many-system step, from a
 //                    shared counter when it runs alone).  The warp lists the
 //                    cell-row runs of the union of its atoms' stencils (the
-//                    x-run of cells in one
-//                    (y, z) row is one contiguous run of sorted atoms), streams
+//                    x-run of cells in one (y, z) row is one contiguous run
+//                    of sorted atoms), streams
 //                    their candidates in full 32-lane chunks, tests each
 //                    against the eight atoms, applies the exclusion window
 //                    bitmask and ballot-compacts the kept atoms straight into
@@ -994,8 +994,9 @@ __device__ __forceinline__ void build_group(const Arena& A, int64_t g, int exclu
 // them one at a time from a shared counter (work_ctl[2], `dynamic` 1), so
 // that a warp that drew cheap groups takes more of them; which warp builds a
 // group does not change its rows.  The force kernel that follows in the same
-// stream clears the queue and the counter.  Complete lists are built a group at a time; REF27 lists (parity
-// only) atom by atom with the reference's own 27-cell stencil.
+// stream clears the queue and the counter.  Complete lists are built a group
+// at a time; REF27 lists (parity only) atom by atom with the reference's own
+// 27-cell stencil.
 __global__ void __launch_bounds__(kNbrThreads, 3) k_nbr_build(Arena A, int64_t n_span, int exclude_exc,
                                                               int dynamic) {
   extern __shared__ __align__(16) unsigned char nbr_smem[];
