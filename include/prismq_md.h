@@ -62,7 +62,7 @@ typedef struct prismq_angle {     /* input.rs:243 AngleParam; U = k (θ - θ0)^2
   float theta0, force_k;
 } prismq_angle;
 
-typedef struct prismq_dihedral {  /* input.rs:541 DihedralParam; U = k (1 + cos(nφ - γ)) */
+typedef struct prismq_dihedral {  /* input.rs:541 DihedralParam; U = k (1 + cos(nφ - γ)), 1 <= n <= 64 */
   int32_t i, j, k, l;
   int32_t periodicity;
   float phase, force_k;

@@ -234,6 +234,12 @@ prismq_status lower_topology(const prismq_topology* T, Lowered* L) {
     const prismq_dihedral& d = T->dihedrals[t];
     if (!in_range(d.i) || !in_range(d.j) || !in_range(d.k) || !in_range(d.l))
       return fail(PRISMQ_E_INVALID, "dihedral " + std::to_string(t) + " has invalid atoms");
+    // the reference's validate rejects periodicity <= 0 (input.rs:2101); the
+    // torsion kernel forms cos and sin of n phi by n steps of a recurrence,
+    // so n is also bounded above
+    if (d.periodicity < 1 || d.periodicity > kMaxPeriodicity)
+      return fail(PRISMQ_E_INVALID, "dihedral " + std::to_string(t) + " has periodicity outside [1, " +
+                                        std::to_string(kMaxPeriodicity) + "]");
     L->dihs.push_back({d.i, d.j, d.k, d.l, d.periodicity, d.phase, d.force_k,
                        (float)std::cos((double)d.phase), (float)std::sin((double)d.phase),
                        ((int)id[d.i].size() & 255) | (((int)id[d.j].size() & 255) << 8) |

@@ -56,6 +56,7 @@ struct AngleT {
   float theta0, kf;
   int pos;  // pos_i | pos_j << 10 | pos_k << 20
 };
+constexpr int kMaxPeriodicity = 64;  // torsion periodicities accepted by the lowering
 struct DihT {
   int i, j, k, l;
   int n;

@@ -292,6 +292,14 @@ def test_invalid_topology_rejected_on_host(gpu, ala40):
     bad2.bonds["j"][0] = ala40.n_atoms + 5
     with pytest.raises(gpu.PrismQError):
         gpu.NhsAmberFusedEngine(bad2, gpu.Params())
+    for per in (0, -2, 65):  # the reference rejects n <= 0; the torsion recurrence bounds n above
+        bad3 = gpu.Topology(ala40.positions, ala40.masses, ala40.charges, ala40.lj_sigma, ala40.lj_epsilon,
+                            ala40.bonds, ala40.angles, ala40.dihedrals.copy(), ala40.exceptions,
+                            ala40.exclusion_offsets, ala40.exclusions, ala40.clusters)
+        bad3.dihedrals["periodicity"][3] = per
+        with pytest.raises(gpu.PrismQError) as e:
+            gpu.NhsAmberFusedEngine(bad3, gpu.Params())
+        assert e.value.status == 1 and "periodicity" in str(e.value)
 
 
 def test_tiny_and_ragged_systems(gpu, orc):
