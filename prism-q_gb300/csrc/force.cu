@@ -276,13 +276,11 @@ __device__ __forceinline__ bool dihedral_out(const R4<R>* pos, const DihT d, Ter
   R sp = lbc * (v0x * c1x + v0y * c1y + v0z * c1z) * inv_n12;
   cp = max_r(R(-1.0f), min_r(R(1.0f), cp));
   sp = max_r(R(-1.0f), min_r(R(1.0f), sp));
-  // cos and sin of n phi (n < 0: sin changes sign)
-  const int n_abs = d.n < 0 ? -d.n : d.n;
-  const R spn = d.n < 0 ? -sp : sp;
+  // cos and sin of n phi (the lowering keeps 1 <= n <= kMaxPeriodicity)
   R cn = R(1.0f), sn = R(0.0f);
-  for (int k = 0; k < n_abs; ++k) {
-    const R c2 = cn * cp - sn * spn;
-    sn = sn * cp + cn * spn;
+  for (int k = 0; k < d.n; ++k) {
+    const R c2 = cn * cp - sn * sp;
+    sn = sn * cp + cn * sp;
     cn = c2;
   }
   const R n = (R)d.n;
