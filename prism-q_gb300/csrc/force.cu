@@ -502,6 +502,10 @@ __global__ void __launch_bounds__(128 * kG, kMinBlocks) k_force(Arena A, int64_t
     skip = !Sp->active || (sel == kSelRebuilding && !Sp->rebuilding) || (sel == kSelBranchA && !Sp->branch_a) ||
            (sel == kSelBranchB && Sp->branch_a);
   }
+  // a block of one group has no partner group to meet at the barriers
+  if constexpr (kG == 1) {
+    if (skip) return;
+  }
   const size_t slot_bytes = (size_t)cap * (3 * sizeof(R) + (kEnergy ? sizeof(double) : 0));
   R* slot_x = reinterpret_cast<R*>(force_smem + sub * slot_bytes);
   R* slot_y = slot_x + cap;
