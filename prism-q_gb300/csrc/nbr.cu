@@ -751,7 +751,10 @@ __device__ bool tile_atom(const Arena& A, const SysDev* Sp, GroupShared& sh, int
 }
 
 // Test one candidate against every atom of the group and append the kept ones
-// to the atoms' rows (ballot compaction keeps candidate order).
+// to the atoms' rows (ballot compaction keeps candidate order).  kCap: test
+// each row against its capacity (the caller skips the tests for a chunk in
+// which no row can reach it).
+template <bool kCap>
 __device__ __forceinline__ void group_test(const Arena& A, const GroupShared& sh, const float4 (&P)[8], int n_act,
                                            int a0, int g, bool valid, int j, float4 pj, float r2max,
                                            int exclude_exc, unsigned lt, int (&cnt)[8], unsigned& ovf) {
@@ -779,7 +782,7 @@ __device__ __forceinline__ void group_test(const Arena& A, const GroupShared& sh
     }
     const unsigned bal = __ballot_sync(0xffffffffu, keep);
     const int add = __popc(bal);
-    if (cnt[i] + add > kNbrCap) {
+    if (kCap && cnt[i] + add > kNbrCap) {
       ovf |= 1u << i;
     } else {
       if (keep) {
@@ -958,10 +961,18 @@ __device__ __forceinline__ void build_group(const Arena& A, int64_t g, int exclu
     const bool valid = c < total;
     const float4 p1 = j1 >= 0 ? A.pos[j1] : make_float4(0.f, 0.f, 0.f, 0.f);
     const int j2 = c + 64 < total ? A.cell_atoms[ab + locate(c + 64)] : -1;
-    if (tiles)
+    if (tiles) {
       tok &= group_test_tiles(A, sh, P, n_act, a0, ab, valid, j, pj, r2max, exclude_exc);
-    else
-      group_test(A, sh, P, n_act, a0, (int)g, valid, j, pj, r2max, exclude_exc, lt, cnt, ovf);
+    } else {
+      // a chunk adds at most 32 entries to a row
+      int most = cnt[0];
+#pragma unroll
+      for (int i = 1; i < 8; ++i) most = max(most, cnt[i]);
+      if (most <= kNbrCap - 32)
+        group_test<false>(A, sh, P, n_act, a0, (int)g, valid, j, pj, r2max, exclude_exc, lt, cnt, ovf);
+      else
+        group_test<true>(A, sh, P, n_act, a0, (int)g, valid, j, pj, r2max, exclude_exc, lt, cnt, ovf);
+    }
     c += 32;
     j = j1;
     pj = p1;
