@@ -377,6 +377,10 @@ prismq_status lower_topology(const prismq_topology* T, Lowered* L) {
         L->far_list.push_back(kv.first | (kv.second ? 0x40000000 : 0));
       }
     }
+    // an atom excludes itself: the group row builder then needs no separate
+    // self test (offset 0 is bit 32 of the window)
+    L->mask_all[a] |= 1ull << 32;
+    L->mask_ref[a] |= 1ull << 32;
     L->far[a] = make_int2(fb, (int)L->far_list.size() - fb);
   }
   // ---- constraint units (fused_engine.rs:11827-11938) ----

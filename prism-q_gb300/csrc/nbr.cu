@@ -753,18 +753,19 @@ __device__ bool tile_atom(const Arena& A, const SysDev* Sp, GroupShared& sh, int
 // Test one candidate against every atom of the group and append the kept ones
 // to the atoms' rows (ballot compaction keeps candidate order).  kCap: test
 // each row against its capacity (the caller skips the tests for a chunk in
-// which no row can reach it).
-template <bool kCap>
+// which no row can reach it); kFull: the group has all eight atoms.  An atom
+// meets itself as a candidate at r^2 = 0 and is dropped by its own window
+// bit (offset 0).
+template <bool kCap, bool kFull>
 __device__ __forceinline__ void group_test(const Arena& A, const GroupShared& sh, const float4 (&P)[8], int n_act,
                                            int a0, int g, bool valid, int j, float4 pj, float r2max,
                                            int exclude_exc, unsigned lt, int (&cnt)[8], unsigned& ovf) {
   int* const rows = A.nbr + (int64_t)g * kNbrCap * 8;  // tiled rows of the group's 8 atoms
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
-    if (i >= n_act) break;
+    if (!kFull && i >= n_act) break;
     const int ai = a0 + i;
-    bool keep = valid && j != ai;
-    if (keep) keep = !(r2_nofma(pj.x - P[i].x, pj.y - P[i].y, pj.z - P[i].z) > r2max);
+    bool keep = valid && !(r2_nofma(pj.x - P[i].x, pj.y - P[i].y, pj.z - P[i].z) > r2max);
     if (keep) {
       const int d = j - ai;
       if (d >= -32 && d < 32) {
@@ -968,10 +969,10 @@ __device__ __forceinline__ void build_group(const Arena& A, int64_t g, int exclu
       int most = cnt[0];
 #pragma unroll
       for (int i = 1; i < 8; ++i) most = max(most, cnt[i]);
-      if (most <= kNbrCap - 32)
-        group_test<false>(A, sh, P, n_act, a0, (int)g, valid, j, pj, r2max, exclude_exc, lt, cnt, ovf);
+      if (most <= kNbrCap - 32 && n_act == 8)
+        group_test<false, true>(A, sh, P, n_act, a0, (int)g, valid, j, pj, r2max, exclude_exc, lt, cnt, ovf);
       else
-        group_test<true>(A, sh, P, n_act, a0, (int)g, valid, j, pj, r2max, exclude_exc, lt, cnt, ovf);
+        group_test<true, false>(A, sh, P, n_act, a0, (int)g, valid, j, pj, r2max, exclude_exc, lt, cnt, ovf);
     }
     c += 32;
     j = j1;

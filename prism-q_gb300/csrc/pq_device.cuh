@@ -157,7 +157,7 @@ struct Arena {
   long long* f = nullptr;  // 3 planes of atom_cap
   double* pe = nullptr;    // 5 planes (bond, angle, dihedral, exception, nonbonded) of atom_cap
   int* atom_sys = nullptr;
-  unsigned long long* mask_all = nullptr;  // exclusion window bits, offsets -32..31
+  unsigned long long* mask_all = nullptr;  // exclusion window bits, offsets -32..31 (offset 0: the atom itself)
   unsigned long long* mask_ref = nullptr;  // same without exception pairs
   int2* far = nullptr;                     // {begin, count} into far_list
   int* far_list = nullptr;                 // partner | (is_exception << 30)
