@@ -753,10 +753,11 @@ __device__ bool tile_atom(const Arena& A, const SysDev* Sp, GroupShared& sh, int
 // Test one candidate against every atom of the group and append the kept ones
 // to the atoms' rows (ballot compaction keeps candidate order).  kCap: test
 // each row against its capacity (the caller skips the tests for a chunk in
-// which no row can reach it); kFull: the group has all eight atoms.  An atom
-// meets itself as a candidate at r^2 = 0 and is dropped by its own window
-// bit (offset 0).
-template <bool kCap, bool kFull>
+// which no row can reach it); kFull: the group has all eight atoms; kFar: some
+// atom of the group has exclusions beyond the ±32 window.  An atom meets
+// itself as a candidate at r^2 = 0 and is dropped by its own window bit
+// (offset 0).
+template <bool kCap, bool kFull, bool kFar>
 __device__ __forceinline__ void group_test(const Arena& A, const GroupShared& sh, const float4 (&P)[8], int n_act,
                                            int a0, int g, bool valid, int j, float4 pj, float r2max,
                                            int exclude_exc, unsigned lt, int (&cnt)[8], unsigned& ovf) {
@@ -770,7 +771,7 @@ __device__ __forceinline__ void group_test(const Arena& A, const GroupShared& sh
       const int d = j - ai;
       if (d >= -32 && d < 32) {
         if ((sh.mask[i] >> (d + 32)) & 1ull) keep = false;
-      } else {
+      } else if (kFar) {
         const int2 far = sh.far[i];
         for (int q = 0; q < far.y; ++q) {
           const int ent = A.far_list[far.x + q];
@@ -859,6 +860,8 @@ __device__ __forceinline__ void build_group(const Arena& A, int64_t g, int exclu
     sh.mask[lane] = exclude_exc ? A.mask_all[a0 + lane] : A.mask_ref[a0 + lane];
     sh.far[lane] = A.far[a0 + lane];
   }
+  // some atom of the group has exclusions beyond its ±32 window
+  const bool far_any = __any_sync(0xffffffffu, lane < n_act && A.far[a0 + min(lane, n_act - 1)].y > 0);
   if (tiles) {
     for (int k = lane; k < kTileHash; k += 32) {
       sh.tkey[k] = 0;
@@ -969,10 +972,10 @@ __device__ __forceinline__ void build_group(const Arena& A, int64_t g, int exclu
       int most = cnt[0];
 #pragma unroll
       for (int i = 1; i < 8; ++i) most = max(most, cnt[i]);
-      if (most <= kNbrCap - 32 && n_act == 8)
-        group_test<false, true>(A, sh, P, n_act, a0, (int)g, valid, j, pj, r2max, exclude_exc, lt, cnt, ovf);
+      if (most <= kNbrCap - 32 && n_act == 8 && !far_any)
+        group_test<false, true, false>(A, sh, P, n_act, a0, (int)g, valid, j, pj, r2max, exclude_exc, lt, cnt, ovf);
       else
-        group_test<true, false>(A, sh, P, n_act, a0, (int)g, valid, j, pj, r2max, exclude_exc, lt, cnt, ovf);
+        group_test<true, false, true>(A, sh, P, n_act, a0, (int)g, valid, j, pj, r2max, exclude_exc, lt, cnt, ovf);
     }
     c += 32;
     j = j1;
